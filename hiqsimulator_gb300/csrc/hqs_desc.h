@@ -1,0 +1,49 @@
+// Descriptors shared by the host engine and the CUDA kernels.
+//
+// A "pass" streams the whole state vector once through shared memory in
+// tiles. A tile is the set of 2^q amplitudes whose indices agree on every
+// state bit outside tile_pos[0..q); tile-local index bit j is state bit
+// tile_pos[j] (ascending, so tile_pos[0..w) == 0..w-1 is the contiguous run
+// that makes global loads coalesced). Every op of the pass acts only on tile
+// bits, so applying the op list tile by tile equals applying each op to the
+// whole state in order.
+#pragma once
+#include <stdint.h>
+
+namespace hqs {
+
+constexpr int kMaxOpsPerPass = 24;
+constexpr int kMaxTileBits = 12;
+constexpr int kMaxK = 5;
+
+// Arithmetic used by the apply kernels.
+enum Arith : int32_t {
+    kArithF64 = 1,  // complex128 storage, native FP64 arithmetic
+    kArithDF = 2,   // complex128 storage, double-float (2 x FP32) arithmetic, ~48-bit
+    kArithF32 = 3,  // complex64 storage, FP32 arithmetic
+};
+
+struct OpDesc {
+    int32_t k;            // targets (0 = scalar multiply of the whole tile)
+    int32_t diag;         // 1: matrix pool holds only the 2^k diagonal entries
+    uint32_t ctrl_local;  // tile-local bits that must all be 1
+    uint32_t mat_off;     // offset (elements) of this op's matrix in the pass pool
+    uint64_t ctrl_outer;  // state bits outside the tile that must all be 1
+    uint8_t tslot[kMaxK]; // tile-local bit of matrix bit j
+    uint8_t pad[3];
+};
+
+struct PassDesc {
+    int32_t n;            // state qubits
+    int32_t q;            // tile bits
+    int32_t w;            // contiguous low run: tile_pos[j] == j for j < w
+    int32_t nops;
+    int32_t nins;         // number of sorted positions in ins_pos
+    uint32_t mat_elems;   // pool elements staged into shared memory
+    uint64_t fixed_mask;  // state bits forced to 1 for every processed tile
+    uint8_t tile_pos[kMaxTileBits];
+    uint8_t ins_pos[64];  // sorted union of tile_pos and fixed-mask positions
+    OpDesc ops[kMaxOpsPerPass];
+};
+
+}  // namespace hqs

@@ -1,0 +1,63 @@
+// Host-side launchers for the state-vector kernels (implemented in
+// kernels.cu). All launches are asynchronous on the given stream; functions
+// returning a value read it back with a synchronous copy on that stream.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "hqs_desc.h"
+
+namespace hqs {
+
+// Reduction scratch: per-CTA partial sums (device) plus a pinned host slot.
+struct ReduceScratch {
+    double* d_partials = nullptr;  // kMaxPartials * 4 doubles
+    double* d_result = nullptr;    // 4 doubles
+    double* h_result = nullptr;    // pinned, 4 doubles
+};
+constexpr int kMaxPartials = 1024;
+
+int device_sm_count();
+
+// One fused pass over the state (see hqs_desc.h). mats: device pool of the
+// pass's matrices in the arithmetic's element format. Returns a cudaError_t.
+cudaError_t launch_pass(int arith, void* state, const void* mats, const PassDesc& d, cudaStream_t s);
+size_t pass_smem_bytes(int arith, const PassDesc& d);
+
+// Sum of |a_i|^2 over indices with (i & mask) == val.
+cudaError_t reduce_probability(int arith, const void* state, int n, uint64_t mask, uint64_t val,
+                               ReduceScratch& rs, cudaStream_t s, double* out);
+// P(bit pos = 0) and P(bit pos = 1) in one sweep.
+cudaError_t reduce_bit_probs(int arith, const void* state, int n, int pos, ReduceScratch& rs,
+                             cudaStream_t s, double* out2);
+// -sum p log2 p.
+cudaError_t reduce_entropy(int arith, const void* state, int n, ReduceScratch& rs, cudaStream_t s,
+                           double* out);
+// nblocks partial sums of |a|^2 over contiguous blocks, written to d_out (device).
+cudaError_t block_sums(int arith, const void* state, int n, uint64_t nblocks, double* d_out, cudaStream_t s);
+// Pauli-sum expectation: sum_t Re(c_t <psi|P_t|psi>); masks/coefs in device memory.
+cudaError_t reduce_pauli_expectation(int arith, const void* state, int n, int nterms, const uint64_t* d_xm,
+                                     const uint64_t* d_ym, const uint64_t* d_zm, const double* d_coef,
+                                     ReduceScratch& rs, cudaStream_t s, double* out);
+
+// out = sum_t c_t P_t in (out-of-place; out and in must not alias). d_coef: per
+// term the pair (c_t i^{|Y_t|}, -c_t i^{|Y_t|}) in the arithmetic's matrix format.
+cudaError_t pauli_apply(int arith, const void* in, void* out, int n, int nterms, const uint64_t* d_xm,
+                        const uint64_t* d_ym, const uint64_t* d_zm, const double* d_coef, cudaStream_t s);
+// Zero amplitudes with (i & mask) != val, scale the others by scale.
+cudaError_t collapse_scale(int arith, void* state, int n, uint64_t mask, uint64_t val, double scale,
+                           cudaStream_t s);
+// Every amplitude := value.
+cudaError_t fill_value(int arith, void* state, uint64_t count, double re, double im, cudaStream_t s);
+// Remove bit pos from the index keeping the half where it equals keep (in place).
+cudaError_t drop_bit(int arith, void* state, int n, int pos, int keep, cudaStream_t s);
+// In-place bit permutation: new state bit newpos[j] takes old bit oldpos[j]
+// (j < m); all other bits stay. {oldpos} and {newpos} are the same set.
+cudaError_t permute_bits(int arith, void* state, int n, int m, const uint8_t* oldpos, const uint8_t* newpos,
+                         cudaStream_t s);
+// complex64 <-> complex128 conversions for host transfers (c64 storage).
+cudaError_t c64_to_c128(const void* in, void* out, uint64_t count, cudaStream_t s);
+cudaError_t c128_to_c64(const void* in, void* out, uint64_t count, cudaStream_t s);
+
+}  // namespace hqs

@@ -1,0 +1,777 @@
+// State-vector kernels for one GB300 (sm_103a).
+//
+// Replaces the reference's OpenMP/AVX2 sweeps (src/simulator-mpi/kernels/
+// {nointrin,intrin}/kernel1..5.hpp, kernels_diag.hpp) and the reductions of
+// src/simulator-mpi/SimulatorMPI.cpp (getProbability_internal :841-870,
+// normalize :872-895, calcLocalApproxDistribution :817-839, Entropy :681-694,
+// DeallocateLocalQubit :278-322) with tiled, coalesced passes over HBM.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "hqs_arith.cuh"
+#include "hqs_kernels.h"
+
+namespace hqs {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ uint64_t insert_zero(uint64_t v, int p) {
+    const uint64_t low = v & ((1ULL << p) - 1ULL);
+    return ((v - low) << 1) | low;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-wide FP64 sum of NV values per thread; result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
+    if (lane == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) red[wid * NV + i] = v[i];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int i = 0; i < NV; ++i) {
+            double s = 0.0;
+            for (int w = 0; w < nw; ++w) s += red[w * NV + i];
+            v[i] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// Fixed-order sum of per-CTA partials (nparts x NV, strided by kMaxPartials).
+template <int NV>
+__global__ void finish_partials(const double* __restrict__ partials, int nparts, double* __restrict__ out) {
+    __shared__ double red[32 * 4];
+    double v[NV];
+#pragma unroll
+    for (int i = 0; i < NV; ++i) v[i] = 0.0;
+    for (int p = threadIdx.x; p < nparts; p += blockDim.x) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) v[i] += partials[i * kMaxPartials + p];
+    }
+    block_sum<NV>(v, red);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; ++i) out[i] = v[i];
+    }
+}
+
+int reduce_grid(uint64_t work) {
+    const uint64_t want = (work + kThreads - 1) / kThreads;
+    int g = device_sm_count() * 4;
+    if ((uint64_t)g > want) g = (int)std::max<uint64_t>(want, 1);
+    return std::min(g, kMaxPartials);
+}
+
+template <int NV>
+cudaError_t finish_reduce(int nparts, ReduceScratch& rs, cudaStream_t s, double* out) {
+    finish_partials<NV><<<1, kThreads, 0, s>>>(rs.d_partials, nparts, rs.d_result);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(rs.h_result, rs.d_result, NV * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    for (int i = 0; i < NV; ++i) out[i] = rs.h_result[i];
+    return cudaSuccess;
+}
+
+// ---------------------------------------------------------------- fused pass
+
+template <class A>
+__device__ __forceinline__ void apply_diag(typename A::store_t* buf, const typename A::mat_t* diag,
+                                           const OpDesc& op, int Q) {
+    for (int L = threadIdx.x; L < Q; L += blockDim.x) {
+        if ((L & op.ctrl_local) != op.ctrl_local) continue;
+        int r = 0;
+        for (int j = 0; j < op.k; ++j) r |= ((L >> op.tslot[j]) & 1) << j;
+        buf[L] = A::mul(diag[r], buf[L]);
+    }
+}
+
+template <class A>
+__device__ __forceinline__ void apply_scalar(typename A::store_t* buf, const typename A::mat_t m, int Q) {
+    for (int L = threadIdx.x; L < Q; L += blockDim.x) buf[L] = A::mul(m, buf[L]);
+}
+
+// Dense k-qubit op, tile src -> tile dst. A task is (index group, block of
+// RPT output rows); consecutive threads take consecutive groups of the same
+// row block so matrix reads are shared-memory broadcasts.
+template <class A, int K>
+__device__ __forceinline__ void apply_dense(const typename A::store_t* __restrict__ src,
+                                            typename A::store_t* __restrict__ dst,
+                                            const typename A::mat_t* __restrict__ mat, const OpDesc& op, int q) {
+    using S = typename A::store_t;
+    constexpr int D = 1 << K;
+    constexpr int RPT = (K >= 3) ? 4 : D;
+    constexpr int LOG_RPT = (K >= 3) ? 2 : K;
+    constexpr int RB = D / RPT;
+    const int gbits = q - K;
+    const int G = 1 << gbits;
+    int ss[K];
+    uint32_t bitv[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        ss[j] = op.tslot[j];
+        bitv[j] = 1u << op.tslot[j];
+    }
+#pragma unroll
+    for (int a = 1; a < K; ++a)
+#pragma unroll
+        for (int b = K - 1; b >= a; --b)
+            if (ss[b - 1] > ss[b]) { const int t = ss[b]; ss[b] = ss[b - 1]; ss[b - 1] = t; }
+
+    for (int task = threadIdx.x; task < G * RB; task += blockDim.x) {
+        const int g = task & (G - 1);
+        const int rb = task >> gbits;
+        uint32_t Lb = (uint32_t)g;
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const uint32_t low = Lb & ((1u << ss[j]) - 1u);
+            Lb = ((Lb - low) << 1) | low;
+        }
+        uint32_t rowoff = 0;  // offset of row rb*RPT
+#pragma unroll
+        for (int j = LOG_RPT; j < K; ++j)
+            if (((rb * RPT) >> j) & 1) rowoff |= bitv[j];
+        if ((Lb & op.ctrl_local) != op.ctrl_local) {
+#pragma unroll
+            for (int rr = 0; rr < RPT; ++rr) {
+                uint32_t o = rowoff;
+#pragma unroll
+                for (int j = 0; j < LOG_RPT; ++j)
+                    if ((rr >> j) & 1) o |= bitv[j];
+                dst[Lb + o] = src[Lb + o];
+            }
+            continue;
+        }
+        typename A::xval x[D];
+#pragma unroll
+        for (int c = 0; c < D; ++c) {
+            uint32_t o = 0;
+#pragma unroll
+            for (int j = 0; j < K; ++j)
+                if ((c >> j) & 1) o |= bitv[j];
+            x[c] = A::load(src[Lb + o]);
+        }
+#pragma unroll
+        for (int rr = 0; rr < RPT; ++rr) {
+            const int r = rb * RPT + rr;
+            const typename A::mat_t* mrow = mat + r * D;
+            typename A::acc_t acc;
+            A::zero(acc);
+#pragma unroll
+            for (int c = 0; c < D; ++c) A::mac(acc, mrow[c], x[c]);
+            uint32_t o = rowoff;
+#pragma unroll
+            for (int j = 0; j < LOG_RPT; ++j)
+                if ((rr >> j) & 1) o |= bitv[j];
+            dst[Lb + o] = A::finish(acc);
+        }
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kThreads) pass_kernel(typename A::store_t* __restrict__ state,
+                                                        const typename A::mat_t* __restrict__ mats,
+                                                        const __grid_constant__ PassDesc d) {
+    using S = typename A::store_t;
+    using M = typename A::mat_t;
+    extern __shared__ __align__(16) unsigned char smem[];
+    M* smat = reinterpret_cast<M*>(smem);
+    const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(M) + 15) & ~(size_t)15;
+    const int Q = 1 << d.q;
+    S* bufA = reinterpret_cast<S*>(smem + mat_bytes);
+    S* bufB = bufA + Q;
+    uint64_t* hoff = reinterpret_cast<uint64_t*>(bufB + Q);
+    const int nh = d.q - d.w;
+    const uint32_t lowmask = (1u << d.w) - 1u;
+
+    for (uint32_t i = threadIdx.x; i < d.mat_elems; i += blockDim.x) smat[i] = mats[i];
+    for (int j = threadIdx.x; j < (1 << nh); j += blockDim.x) {
+        uint64_t o = 0;
+        for (int b = 0; b < nh; ++b)
+            if ((j >> b) & 1) o |= 1ULL << d.tile_pos[d.w + b];
+        hoff[j] = o;
+    }
+    __syncthreads();
+
+    const uint64_t ntiles = 1ULL << (d.n - d.nins);
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        uint64_t base = t;
+        for (int i = 0; i < d.nins; ++i) base = insert_zero(base, d.ins_pos[i]);
+        base |= d.fixed_mask;
+        for (int L = threadIdx.x; L < Q; L += blockDim.x)
+            bufA[L] = state[base + hoff[L >> d.w] + (L & lowmask)];
+        __syncthreads();
+        S* src = bufA;
+        S* dst = bufB;
+        for (int oi = 0; oi < d.nops; ++oi) {
+            const OpDesc& op = d.ops[oi];
+            if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
+            if (op.k == 0) {
+                apply_scalar<A>(src, smat[op.mat_off], Q);
+                __syncthreads();
+                continue;
+            }
+            if (op.diag) {
+                apply_diag<A>(src, smat + op.mat_off, op, Q);
+                __syncthreads();
+                continue;
+            }
+            switch (op.k) {
+                case 1: apply_dense<A, 1>(src, dst, smat + op.mat_off, op, d.q); break;
+                case 2: apply_dense<A, 2>(src, dst, smat + op.mat_off, op, d.q); break;
+                case 3: apply_dense<A, 3>(src, dst, smat + op.mat_off, op, d.q); break;
+                case 4: apply_dense<A, 4>(src, dst, smat + op.mat_off, op, d.q); break;
+                default: apply_dense<A, 5>(src, dst, smat + op.mat_off, op, d.q); break;
+            }
+            __syncthreads();
+            S* tmp = src;
+            src = dst;
+            dst = tmp;
+        }
+        for (int L = threadIdx.x; L < Q; L += blockDim.x)
+            state[base + hoff[L >> d.w] + (L & lowmask)] = src[L];
+        __syncthreads();
+    }
+}
+
+template <class A>
+size_t pass_smem_t(const PassDesc& d) {
+    const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(typename A::mat_t) + 15) & ~(size_t)15;
+    return mat_bytes + 2 * (sizeof(typename A::store_t) << d.q) + sizeof(uint64_t) * (1u << (d.q - d.w));
+}
+
+template <class A>
+cudaError_t launch_pass_t(void* state, const void* mats, const PassDesc& d, cudaStream_t s) {
+    const size_t smem = pass_smem_t<A>(d);
+    auto kern = pass_kernel<A>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const uint64_t ntiles = 1ULL << (d.n - d.nins);
+    uint64_t grid = (uint64_t)device_sm_count() * per_sm;
+    if (grid > ntiles) grid = ntiles;
+    kern<<<(unsigned)grid, kThreads, smem, s>>>(reinterpret_cast<typename A::store_t*>(state),
+                                                 reinterpret_cast<const typename A::mat_t*>(mats), d);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------- reductions
+
+struct MaskSpec {
+    uint64_t val;
+    int npos;
+    uint8_t pos[64];  // sorted positions of mask bits
+};
+
+template <class NA, class S>
+__global__ void __launch_bounds__(kThreads) probability_kernel(const S* __restrict__ state, uint64_t count,
+                                                               const __grid_constant__ MaskSpec m,
+                                                               double* __restrict__ partials) {
+    __shared__ double red[32];
+    NA acc;
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t i = j;
+        for (int b = 0; b < m.npos; ++b) i = insert_zero(i, m.pos[b]);
+        acc.add(state[i | m.val]);
+    }
+    double v[1] = {acc.value()};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
+}
+
+template <class NA, class S>
+__global__ void __launch_bounds__(kThreads) bit_probs_kernel(const S* __restrict__ state, uint64_t count, int pos,
+                                                             double* __restrict__ partials) {
+    __shared__ double red[64];
+    NA a0, a1;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if ((i >> pos) & 1ULL) a1.add(state[i]);
+        else a0.add(state[i]);
+    }
+    double v[2] = {a0.value(), a1.value()};
+    block_sum<2>(v, red);
+    if (threadIdx.x == 0) {
+        partials[blockIdx.x] = v[0];
+        partials[kMaxPartials + blockIdx.x] = v[1];
+    }
+}
+
+template <class NA, class S>
+__global__ void __launch_bounds__(kThreads) entropy_kernel(const S* __restrict__ state, uint64_t count,
+                                                           double* __restrict__ partials) {
+    __shared__ double red[32];
+    double e = 0.0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        NA a;
+        a.add(state[i]);
+        const double p = a.value();
+        if (p > 0.0) e += p * log2(p);
+    }
+    double v[1] = {e};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
+}
+
+// Block sums for measurement: one CTA per block when blocks are large, one
+// thread per block (summing in index order) when they are small.
+template <class NA, class S>
+__global__ void __launch_bounds__(kThreads) block_sum_cta_kernel(const S* __restrict__ state, uint64_t K,
+                                                                 double* __restrict__ out) {
+    __shared__ double red[32];
+    NA acc;
+    const uint64_t b0 = (uint64_t)blockIdx.x * K;
+    for (uint64_t j = threadIdx.x; j < K; j += blockDim.x) acc.add(state[b0 + j]);
+    double v[1] = {acc.value()};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) out[blockIdx.x] = v[0];
+}
+
+template <class NA, class S>
+__global__ void __launch_bounds__(kThreads) block_sum_serial_kernel(const S* __restrict__ state, uint64_t K,
+                                                                    uint64_t nblocks, double* __restrict__ out) {
+    const uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (b >= nblocks) return;
+    double s = 0.0;
+    for (uint64_t j = 0; j < K; ++j) {
+        NA a;
+        a.add(state[b * K + j]);
+        s += a.value();
+    }
+    out[b] = s;
+}
+
+// Pauli expectation: sum_t Re(c_t * sum_i conj(a_i) phase_t(j) a_j), j = i ^ x_t,
+// phase_t(j) = i^{|Y_t|} (-1)^{popcount(j & (Y_t|Z_t))}.
+template <class S>
+__device__ __forceinline__ void load_d2(const S* st, uint64_t i, double& re, double& im);
+template <>
+__device__ __forceinline__ void load_d2<double2>(const double2* st, uint64_t i, double& re, double& im) {
+    const double2 v = st[i];
+    re = v.x;
+    im = v.y;
+}
+template <>
+__device__ __forceinline__ void load_d2<float2>(const float2* st, uint64_t i, double& re, double& im) {
+    const float2 v = st[i];
+    re = v.x;
+    im = v.y;
+}
+
+template <class S>
+__global__ void __launch_bounds__(kThreads) pauli_expect_kernel(const S* __restrict__ state, uint64_t count,
+                                                                int nterms, const uint64_t* __restrict__ xm,
+                                                                const uint64_t* __restrict__ ym,
+                                                                const uint64_t* __restrict__ zm,
+                                                                const double* __restrict__ coef,
+                                                                double* __restrict__ partials) {
+    __shared__ double red[32];
+    double total = 0.0;
+    for (int t = 0; t < nterms; ++t) {
+        const uint64_t x = xm[t], yz = ym[t] | zm[t];
+        const int ny = __popcll(ym[t]) & 3;
+        NormAccDF sre, sim;  // double-float accumulators of the real / imaginary sums
+        for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+             i += (uint64_t)gridDim.x * blockDim.x) {
+            const uint64_t j = i ^ x;
+            double ar, ai, br, bi;
+            load_d2<S>(state, i, ar, ai);
+            load_d2<S>(state, j, br, bi);
+            if (__popcll(j & yz) & 1) { br = -br; bi = -bi; }
+            // conj(a) * b = (ar br + ai bi) + i (ar bi - ai br), each product split exactly
+            const DF arf = df_split(ar), aif = df_split(ai), brf = df_split(br), bif = df_split(bi);
+            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
+            df_mac(rh, rl, arf.h, arf.l, brf.h, brf.l);
+            df_mac(rh, rl, aif.h, aif.l, bif.h, bif.l);
+            df_mac(ih, il, arf.h, arf.l, bif.h, bif.l);
+            df_mac(ih, il, -aif.h, -aif.l, brf.h, brf.l);
+            // accumulate (rh + rl) and (ih + il)
+            float s = sre.h + rh, bb = s - sre.h;
+            sre.l += ((sre.h - (s - bb)) + (rh - bb)) + rl;
+            sre.h = s;
+            s = sim.h + ih;
+            bb = s - sim.h;
+            sim.l += ((sim.h - (s - bb)) + (ih - bb)) + il;
+            sim.h = s;
+        }
+        // multiply by i^ny, then take Re(c * .)
+        double re = sre.value(), im = sim.value();
+        for (int r = 0; r < ny; ++r) {
+            const double tr = -im;
+            im = re;
+            re = tr;
+        }
+        total += coef[2 * t] * re - coef[2 * t + 1] * im;
+    }
+    double v[1] = {total};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
+}
+
+// out_i = sum_t c_t phase_t(j) a_j with j = i ^ x_t. coef holds two entries
+// per term in the arithmetic's matrix format: c_t i^{|Y_t|} and its negation,
+// selected by the parity of j & (Y_t | Z_t).
+template <class A>
+__global__ void __launch_bounds__(kThreads) pauli_apply_kernel(const typename A::store_t* __restrict__ in,
+                                                               typename A::store_t* __restrict__ out, uint64_t count,
+                                                               int nterms, const uint64_t* __restrict__ xm,
+                                                               const uint64_t* __restrict__ ym,
+                                                               const uint64_t* __restrict__ zm,
+                                                               const typename A::mat_t* __restrict__ coef) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        typename A::acc_t acc;
+        A::zero(acc);
+        for (int t = 0; t < nterms; ++t) {
+            const uint64_t j = i ^ xm[t];
+            const int neg = __popcll(j & (ym[t] | zm[t])) & 1;
+            A::mac(acc, coef[2 * t + neg], A::load(in[j]));
+        }
+        out[i] = A::finish(acc);
+    }
+}
+
+template <class A>
+__global__ void __launch_bounds__(kThreads) collapse_kernel(typename A::store_t* __restrict__ state, uint64_t count,
+                                                            uint64_t mask, uint64_t val,
+                                                            const typename A::mat_t scale) {
+    using S = typename A::store_t;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        if ((i & mask) != val) {
+            S z;
+            z.x = 0;
+            z.y = 0;
+            state[i] = z;
+        } else {
+            state[i] = A::mul(scale, state[i]);
+        }
+    }
+}
+
+template <class S>
+__global__ void fill_kernel(S* __restrict__ state, uint64_t count, S v) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        state[i] = v;
+}
+
+// new[i] = old[src(i)] for i in [lo, hi); sources are disjoint from [lo, hi).
+template <class S>
+__global__ void drop_bit_kernel(S* __restrict__ state, uint64_t lo, uint64_t hi, int pos, uint64_t keepbit) {
+    const uint64_t lowm = (1ULL << pos) - 1ULL;
+    for (uint64_t i = lo + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < hi;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t src = ((i & ~lowm) << 1) | (i & lowm) | keepbit;
+        state[i] = state[src];
+    }
+}
+
+struct PermSpec {
+    int n, q, w, nins;
+    uint8_t tile_pos[kMaxTileBits];
+    uint8_t ins_pos[64];
+    uint8_t src_slot[kMaxTileBits];  // for destination tile bit j: source tile bit
+};
+
+// In-place bit permutation, one tile at a time: every tile maps onto itself.
+template <class S>
+__global__ void __launch_bounds__(kThreads) permute_kernel(S* __restrict__ state, const __grid_constant__ PermSpec p) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int Q = 1 << p.q;
+    S* buf = reinterpret_cast<S*>(smem);
+    uint64_t* hoff = reinterpret_cast<uint64_t*>(buf + Q);
+    const int nh = p.q - p.w;
+    const uint32_t lowmask = (1u << p.w) - 1u;
+    for (int j = threadIdx.x; j < (1 << nh); j += blockDim.x) {
+        uint64_t o = 0;
+        for (int b = 0; b < nh; ++b)
+            if ((j >> b) & 1) o |= 1ULL << p.tile_pos[p.w + b];
+        hoff[j] = o;
+    }
+    __syncthreads();
+    const uint64_t ntiles = 1ULL << (p.n - p.nins);
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        uint64_t base = t;
+        for (int i = 0; i < p.nins; ++i) base = insert_zero(base, p.ins_pos[i]);
+        for (int L = threadIdx.x; L < Q; L += blockDim.x) buf[L] = state[base + hoff[L >> p.w] + (L & lowmask)];
+        __syncthreads();
+        for (int L = threadIdx.x; L < Q; L += blockDim.x) {
+            int Ls = 0;
+            for (int j = 0; j < p.q; ++j) Ls |= ((L >> j) & 1) << p.src_slot[j];
+            state[base + hoff[L >> p.w] + (L & lowmask)] = buf[Ls];
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void c64_to_c128_kernel(const float2* __restrict__ in, double2* __restrict__ out, uint64_t count) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = make_double2((double)in[i].x, (double)in[i].y);
+}
+__global__ void c128_to_c64_kernel(const double2* __restrict__ in, float2* __restrict__ out, uint64_t count) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
+         i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = make_float2((float)in[i].x, (float)in[i].y);
+}
+
+int stream_grid(uint64_t count) {
+    const uint64_t want = (count + kThreads - 1) / kThreads;
+    const uint64_t cap = (uint64_t)device_sm_count() * 8;
+    return (int)std::max<uint64_t>(1, std::min(want, cap));
+}
+
+MaskSpec make_mask_spec(uint64_t mask, uint64_t val) {
+    MaskSpec m;
+    m.val = val;
+    m.npos = 0;
+    for (int b = 0; b < 64; ++b)
+        if ((mask >> b) & 1ULL) m.pos[m.npos++] = (uint8_t)b;
+    return m;
+}
+
+}  // namespace
+
+int device_sm_count() {
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    return sms;
+}
+
+size_t pass_smem_bytes(int arith, const PassDesc& d) {
+    switch (arith) {
+        case kArithF64: return pass_smem_t<ArithF64>(d);
+        case kArithDF: return pass_smem_t<ArithDF>(d);
+        default: return pass_smem_t<ArithF32>(d);
+    }
+}
+
+cudaError_t launch_pass(int arith, void* state, const void* mats, const PassDesc& d, cudaStream_t s) {
+    switch (arith) {
+        case kArithF64: return launch_pass_t<ArithF64>(state, mats, d, s);
+        case kArithDF: return launch_pass_t<ArithDF>(state, mats, d, s);
+        case kArithF32: return launch_pass_t<ArithF32>(state, mats, d, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t reduce_probability(int arith, const void* state, int n, uint64_t mask, uint64_t val,
+                               ReduceScratch& rs, cudaStream_t s, double* out) {
+    const MaskSpec m = make_mask_spec(mask, val);
+    const uint64_t count = (1ULL << n) >> m.npos;
+    const int g = reduce_grid(count);
+    if (arith == kArithF64)
+        probability_kernel<NormAccF64, double2><<<g, kThreads, 0, s>>>((const double2*)state, count, m, rs.d_partials);
+    else if (arith == kArithDF)
+        probability_kernel<NormAccDF, double2><<<g, kThreads, 0, s>>>((const double2*)state, count, m, rs.d_partials);
+    else
+        probability_kernel<NormAccDF, float2><<<g, kThreads, 0, s>>>((const float2*)state, count, m, rs.d_partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return finish_reduce<1>(g, rs, s, out);
+}
+
+cudaError_t reduce_bit_probs(int arith, const void* state, int n, int pos, ReduceScratch& rs, cudaStream_t s,
+                             double* out2) {
+    const uint64_t count = 1ULL << n;
+    const int g = reduce_grid(count);
+    if (arith == kArithF64)
+        bit_probs_kernel<NormAccF64, double2><<<g, kThreads, 0, s>>>((const double2*)state, count, pos, rs.d_partials);
+    else if (arith == kArithDF)
+        bit_probs_kernel<NormAccDF, double2><<<g, kThreads, 0, s>>>((const double2*)state, count, pos, rs.d_partials);
+    else
+        bit_probs_kernel<NormAccDF, float2><<<g, kThreads, 0, s>>>((const float2*)state, count, pos, rs.d_partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return finish_reduce<2>(g, rs, s, out2);
+}
+
+cudaError_t reduce_entropy(int arith, const void* state, int n, ReduceScratch& rs, cudaStream_t s, double* out) {
+    const uint64_t count = 1ULL << n;
+    const int g = reduce_grid(count);
+    if (arith == kArithF64)
+        entropy_kernel<NormAccF64, double2><<<g, kThreads, 0, s>>>((const double2*)state, count, rs.d_partials);
+    else if (arith == kArithDF)
+        entropy_kernel<NormAccDF, double2><<<g, kThreads, 0, s>>>((const double2*)state, count, rs.d_partials);
+    else
+        entropy_kernel<NormAccDF, float2><<<g, kThreads, 0, s>>>((const float2*)state, count, rs.d_partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = finish_reduce<1>(g, rs, s, out);
+    if (e == cudaSuccess) *out = -*out;
+    return e;
+}
+
+cudaError_t block_sums(int arith, const void* state, int n, uint64_t nblocks, double* d_out, cudaStream_t s) {
+    const uint64_t K = (1ULL << n) / nblocks;
+    if (K >= kThreads) {
+        if (arith == kArithF64)
+            block_sum_cta_kernel<NormAccF64, double2><<<(unsigned)nblocks, kThreads, 0, s>>>((const double2*)state, K, d_out);
+        else if (arith == kArithDF)
+            block_sum_cta_kernel<NormAccDF, double2><<<(unsigned)nblocks, kThreads, 0, s>>>((const double2*)state, K, d_out);
+        else
+            block_sum_cta_kernel<NormAccDF, float2><<<(unsigned)nblocks, kThreads, 0, s>>>((const float2*)state, K, d_out);
+    } else {
+        const unsigned g = (unsigned)((nblocks + kThreads - 1) / kThreads);
+        if (arith == kArithF64)
+            block_sum_serial_kernel<NormAccF64, double2><<<g, kThreads, 0, s>>>((const double2*)state, K, nblocks, d_out);
+        else if (arith == kArithDF)
+            block_sum_serial_kernel<NormAccDF, double2><<<g, kThreads, 0, s>>>((const double2*)state, K, nblocks, d_out);
+        else
+            block_sum_serial_kernel<NormAccDF, float2><<<g, kThreads, 0, s>>>((const float2*)state, K, nblocks, d_out);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t reduce_pauli_expectation(int arith, const void* state, int n, int nterms, const uint64_t* d_xm,
+                                     const uint64_t* d_ym, const uint64_t* d_zm, const double* d_coef,
+                                     ReduceScratch& rs, cudaStream_t s, double* out) {
+    const uint64_t count = 1ULL << n;
+    const int g = reduce_grid(count);
+    if (arith == kArithF32)
+        pauli_expect_kernel<float2><<<g, kThreads, 0, s>>>((const float2*)state, count, nterms, d_xm, d_ym, d_zm,
+                                                           d_coef, rs.d_partials);
+    else
+        pauli_expect_kernel<double2><<<g, kThreads, 0, s>>>((const double2*)state, count, nterms, d_xm, d_ym, d_zm,
+                                                            d_coef, rs.d_partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return finish_reduce<1>(g, rs, s, out);
+}
+
+cudaError_t pauli_apply(int arith, const void* in, void* out, int n, int nterms, const uint64_t* d_xm,
+                        const uint64_t* d_ym, const uint64_t* d_zm, const double* d_coef, cudaStream_t s) {
+    const uint64_t count = 1ULL << n;
+    const int g = stream_grid(count);
+    if (arith == kArithF64)
+        pauli_apply_kernel<ArithF64><<<g, kThreads, 0, s>>>((const double2*)in, (double2*)out, count, nterms, d_xm,
+                                                             d_ym, d_zm, (const double2*)d_coef);  // 2 x double2 per term
+    else if (arith == kArithDF)
+        pauli_apply_kernel<ArithDF><<<g, kThreads, 0, s>>>((const double2*)in, (double2*)out, count, nterms, d_xm,
+                                                            d_ym, d_zm, (const float4*)d_coef);
+    else
+        pauli_apply_kernel<ArithF32><<<g, kThreads, 0, s>>>((const float2*)in, (float2*)out, count, nterms, d_xm,
+                                                             d_ym, d_zm, (const float2*)d_coef);
+    return cudaGetLastError();
+}
+
+cudaError_t collapse_scale(int arith, void* state, int n, uint64_t mask, uint64_t val, double scale,
+                           cudaStream_t s) {
+    const uint64_t count = 1ULL << n;
+    const int g = stream_grid(count);
+    if (arith == kArithF64) {
+        collapse_kernel<ArithF64><<<g, kThreads, 0, s>>>((double2*)state, count, mask, val, make_double2(scale, 0.0));
+    } else if (arith == kArithDF) {
+        const float h = (float)scale;
+        const float l = (float)(scale - (double)h);
+        collapse_kernel<ArithDF><<<g, kThreads, 0, s>>>((double2*)state, count, mask, val, make_float4(h, 0.f, l, 0.f));
+    } else {
+        collapse_kernel<ArithF32><<<g, kThreads, 0, s>>>((float2*)state, count, mask, val,
+                                                         make_float2((float)scale, 0.f));
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t fill_value(int arith, void* state, uint64_t count, double re, double im, cudaStream_t s) {
+    const int g = stream_grid(count);
+    if (arith == kArithF32)
+        fill_kernel<float2><<<g, kThreads, 0, s>>>((float2*)state, count, make_float2((float)re, (float)im));
+    else
+        fill_kernel<double2><<<g, kThreads, 0, s>>>((double2*)state, count, make_double2(re, im));
+    return cudaGetLastError();
+}
+
+cudaError_t drop_bit(int arith, void* state, int n, int pos, int keep, cudaStream_t s) {
+    // windows [lo, hi) whose sources lie entirely above hi (see kernel comment)
+    const uint64_t keepbit = keep ? (1ULL << pos) : 0ULL;
+    const uint64_t half = 1ULL << (n - 1);
+    auto run = [&](uint64_t lo, uint64_t hi) -> cudaError_t {
+        const int g = stream_grid(hi - lo);
+        if (arith == kArithF32) drop_bit_kernel<float2><<<g, kThreads, 0, s>>>((float2*)state, lo, hi, pos, keepbit);
+        else drop_bit_kernel<double2><<<g, kThreads, 0, s>>>((double2*)state, lo, hi, pos, keepbit);
+        return cudaGetLastError();
+    };
+    cudaError_t e = cudaSuccess;
+    if (keep) e = run(0, std::min<uint64_t>(1ULL << pos, half));
+    for (int j = pos; j < n - 1 && e == cudaSuccess; ++j) e = run(1ULL << j, std::min<uint64_t>(1ULL << (j + 1), half));
+    return e;
+}
+
+cudaError_t permute_bits(int arith, void* state, int n, int m, const uint8_t* oldpos, const uint8_t* newpos,
+                         cudaStream_t s) {
+    if (m == 0) return cudaSuccess;
+    PermSpec p;
+    p.n = n;
+    // tile: the permuted positions plus the lowest other positions, up to 2^10
+    // amplitudes (or the whole state)
+    uint64_t inset = 0;
+    for (int j = 0; j < m; ++j) inset |= 1ULL << oldpos[j];
+    int q = std::min(n, std::max(m, 10));
+    if (q > kMaxTileBits) return cudaErrorInvalidValue;
+    for (int b = 0; b < n && __builtin_popcountll(inset) < q; ++b) inset |= 1ULL << b;
+    q = __builtin_popcountll(inset);
+    p.q = q;
+    int c = 0;
+    for (int b = 0; b < n; ++b)
+        if ((inset >> b) & 1ULL) p.tile_pos[c++] = (uint8_t)b;
+    p.w = 0;
+    while (p.w < q && p.tile_pos[p.w] == p.w) ++p.w;
+    p.nins = q;
+    for (int j = 0; j < q; ++j) p.ins_pos[j] = p.tile_pos[j];
+    int slot[64];
+    for (int j = 0; j < q; ++j) slot[p.tile_pos[j]] = j;
+    for (int j = 0; j < q; ++j) p.src_slot[j] = (uint8_t)j;
+    for (int j = 0; j < m; ++j) p.src_slot[slot[newpos[j]]] = (uint8_t)slot[oldpos[j]];
+    const size_t elem = (arith == kArithF32) ? sizeof(float2) : sizeof(double2);
+    const size_t smem = (elem << q) + sizeof(uint64_t) * (1u << (q - p.w));
+    const uint64_t ntiles = 1ULL << (n - q);
+    const unsigned g = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)device_sm_count() * 4);
+    if (arith == kArithF32) {
+        cudaFuncSetAttribute(permute_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        permute_kernel<float2><<<g, kThreads, smem, s>>>((float2*)state, p);
+    } else {
+        cudaFuncSetAttribute(permute_kernel<double2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        permute_kernel<double2><<<g, kThreads, smem, s>>>((double2*)state, p);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t c64_to_c128(const void* in, void* out, uint64_t count, cudaStream_t s) {
+    c64_to_c128_kernel<<<stream_grid(count), kThreads, 0, s>>>((const float2*)in, (double2*)out, count);
+    return cudaGetLastError();
+}
+cudaError_t c128_to_c64(const void* in, void* out, uint64_t count, cudaStream_t s) {
+    c128_to_c64_kernel<<<stream_grid(count), kThreads, 0, s>>>((const double2*)in, (float2*)out, count);
+    return cudaGetLastError();
+}
+
+}  // namespace hqs

@@ -1,0 +1,226 @@
+#include "workspace.h"
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+namespace hqs {
+
+void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) throw CudaError(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+}
+
+Workspace::Workspace() {
+    cuda_check(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaMalloc(&rs_.d_partials, sizeof(double) * kMaxPartials * 4), "cudaMalloc(partials)");
+    cuda_check(cudaMalloc(&rs_.d_result, sizeof(double) * 4), "cudaMalloc(result)");
+    cuda_check(cudaMallocHost(&rs_.h_result, sizeof(double) * 4), "cudaMallocHost(result)");
+    cuda_check(cudaEventCreateWithFlags(&staging_free_, cudaEventDisableTiming), "cudaEventCreate");
+}
+
+Workspace::~Workspace() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    cudaFree(rs_.d_partials);
+    cudaFree(rs_.d_result);
+    cudaFreeHost(rs_.h_result);
+    cudaFree(pool_);
+    cudaFreeHost(pinned_);
+    cudaFree(scratch_);
+    cudaFree(up_);
+    if (staging_free_) cudaEventDestroy(staging_free_);
+    if (stream_) cudaStreamDestroy(stream_);
+}
+
+void* Workspace::scratch(size_t bytes) {
+    if (bytes > scratch_bytes_) {
+        cuda_check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        cudaFree(scratch_);
+        scratch_ = nullptr;
+        scratch_bytes_ = 0;
+        cuda_check(cudaMalloc(&scratch_, bytes), "cudaMalloc(scratch)");
+        scratch_bytes_ = bytes;
+    }
+    return scratch_;
+}
+
+void* Workspace::upload(const void* host, size_t bytes) {
+    if (bytes > up_bytes_) {
+        cuda_check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+        cudaFree(up_);
+        up_ = nullptr;
+        up_bytes_ = 0;
+        const size_t cap = std::max<size_t>(bytes, 4096);
+        cuda_check(cudaMalloc(&up_, cap), "cudaMalloc(upload)");
+        up_bytes_ = cap;
+    }
+    cuda_check(cudaMemcpyAsync(up_, host, bytes, cudaMemcpyHostToDevice, stream_), "cudaMemcpyAsync(upload)");
+    // the host source may be reused by the caller right after return
+    cuda_check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    return up_;
+}
+
+void Workspace::ensure_pool(size_t bytes) {
+    if (bytes <= pool_bytes_) return;
+    cuda_check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    cudaFree(pool_);
+    pool_ = nullptr;
+    pool_bytes_ = 0;
+    const size_t cap = std::max<size_t>(bytes * 2, 1 << 20);
+    cuda_check(cudaMalloc(&pool_, cap), "cudaMalloc(matrix pool)");
+    pool_bytes_ = cap;
+}
+
+void Workspace::ensure_pinned(size_t bytes) {
+    if (staging_pending_) {
+        cuda_check(cudaEventSynchronize(staging_free_), "cudaEventSynchronize");
+        staging_pending_ = false;
+    }
+    if (bytes <= pinned_bytes_) return;
+    cudaFreeHost(pinned_);
+    pinned_ = nullptr;
+    pinned_bytes_ = 0;
+    const size_t cap = std::max<size_t>(bytes * 2, 1 << 20);
+    cuda_check(cudaMallocHost(&pinned_, cap), "cudaMallocHost(staging)");
+    pinned_bytes_ = cap;
+}
+
+static int popc64(uint64_t v) { return __builtin_popcountll(v); }
+
+std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits, int max_ops,
+                                  std::vector<size_t>* op_first) {
+    const size_t melem = Workspace::mat_elem_bytes(arith);
+    const size_t store = (arith == kArithF32) ? 8 : 16;
+    const size_t mat_budget = 64 * 1024;
+    max_tile_bits = std::max(5, std::min(max_tile_bits, kMaxTileBits));
+    max_ops = std::max(1, std::min(max_ops, kMaxOpsPerPass));
+    std::vector<PassPlan> plans;
+    size_t i = 0, pool_off = 0;
+    while (i < ops.size()) {
+        uint64_t tset = 0;
+        size_t mbytes = 0, j = i;
+        if (op_first) op_first->push_back(i);
+        while (j < ops.size() && (int)(j - i) < max_ops) {
+            const GateOp& op = ops[j];
+            uint64_t tm = 0;
+            for (int t = 0; t < op.k; ++t) tm |= 1ULL << op.pos[t];
+            const uint64_t ns = tset | tm;
+            const size_t ob = op.m.size() * melem;
+            if (j > i && (popc64(ns) + 4 > max_tile_bits || mbytes + ob > mat_budget)) break;
+            tset = ns;
+            mbytes += ob;
+            ++j;
+        }
+        PassPlan pl;
+        PassDesc& d = pl.desc;
+        std::memset(&d, 0, sizeof(d));
+        const int q = std::min(n, std::max(popc64(tset), max_tile_bits));
+        uint64_t tile = tset;
+        for (int b = 0; b < n && popc64(tile) < q; ++b) tile |= 1ULL << b;
+        int slot[64];
+        int c = 0;
+        for (int b = 0; b < n; ++b)
+            if ((tile >> b) & 1ULL) {
+                slot[b] = c;
+                d.tile_pos[c++] = (uint8_t)b;
+            }
+        d.n = n;
+        d.q = q;
+        d.w = 0;
+        while (d.w < q && d.tile_pos[d.w] == d.w) ++d.w;
+        uint64_t fixed = ~0ULL;
+        for (size_t o = i; o < j; ++o) fixed &= ops[o].ctrl_mask & ~tile;
+        if (j == i) fixed = 0;
+        d.fixed_mask = fixed;
+        const uint64_t ins = tile | fixed;
+        d.nins = 0;
+        for (int b = 0; b < 64; ++b)
+            if ((ins >> b) & 1ULL) d.ins_pos[d.nins++] = (uint8_t)b;
+        d.nops = (int)(j - i);
+        uint32_t moff = 0;
+        for (size_t o = i; o < j; ++o) {
+            const GateOp& op = ops[o];
+            OpDesc& od = d.ops[o - i];
+            od.k = op.k;
+            od.diag = op.diag ? 1 : 0;
+            od.ctrl_outer = op.ctrl_mask & ~tile;
+            uint32_t cl = 0;
+            for (int b = 0; b < n; ++b)
+                if (((op.ctrl_mask & tile) >> b) & 1ULL) cl |= 1u << slot[b];
+            od.ctrl_local = cl;
+            for (int t = 0; t < op.k; ++t) od.tslot[t] = (uint8_t)slot[op.pos[t]];
+            od.mat_off = moff;
+            moff += (uint32_t)op.m.size();
+        }
+        d.mat_elems = moff;
+        pl.pool_off = pool_off;
+        pool_off += ((size_t)moff * melem + 255) & ~(size_t)255;
+        pl.bytes = 2ULL * (1ULL << (n - popc64(fixed))) * store;
+        plans.push_back(pl);
+        i = j;
+    }
+    return plans;
+}
+
+static void convert_matrix(int arith, const std::vector<cplx>& m, unsigned char* dst) {
+    if (arith == kArithF64) {
+        double* p = reinterpret_cast<double*>(dst);
+        for (size_t e = 0; e < m.size(); ++e) {
+            p[2 * e] = m[e].real();
+            p[2 * e + 1] = m[e].imag();
+        }
+    } else if (arith == kArithDF) {
+        float* p = reinterpret_cast<float*>(dst);
+        for (size_t e = 0; e < m.size(); ++e) {
+            const double re = m[e].real(), im = m[e].imag();
+            const float hr = (float)re, hi = (float)im;
+            p[4 * e] = hr;
+            p[4 * e + 1] = hi;
+            p[4 * e + 2] = (float)(re - (double)hr);
+            p[4 * e + 3] = (float)(im - (double)hi);
+        }
+    } else {
+        float* p = reinterpret_cast<float*>(dst);
+        for (size_t e = 0; e < m.size(); ++e) {
+            p[2 * e] = (float)m[e].real();
+            p[2 * e + 1] = (float)m[e].imag();
+        }
+    }
+}
+
+uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits,
+                              int max_ops, uint64_t* passes_out) {
+    if (ops.empty()) return 0;
+    std::vector<size_t> first;
+    std::vector<PassPlan> plans = plan_passes(n, arith, ops, max_tile_bits, max_ops, &first);
+    size_t total = 0;
+    for (const auto& p : plans) {
+        const size_t end = p.pool_off + ((size_t)p.desc.mat_elems * mat_elem_bytes(arith) + 255) / 256 * 256;
+        total = std::max(total, end);
+    }
+    total = std::max<size_t>(total, 256);
+    ensure_pinned(total);
+    ensure_pool(total);
+    unsigned char* host = static_cast<unsigned char*>(pinned_);
+    for (size_t pi = 0; pi < plans.size(); ++pi) {
+        const PassPlan& p = plans[pi];
+        size_t off = p.pool_off;
+        for (int o = 0; o < p.desc.nops; ++o) {
+            const GateOp& op = ops[first[pi] + o];
+            convert_matrix(arith, op.m, host + off);
+            off += op.m.size() * mat_elem_bytes(arith);
+        }
+    }
+    cuda_check(cudaMemcpyAsync(pool_, pinned_, total, cudaMemcpyHostToDevice, stream_), "cudaMemcpyAsync(matrices)");
+    cuda_check(cudaEventRecord(staging_free_, stream_), "cudaEventRecord");
+    staging_pending_ = true;
+    uint64_t bytes = 0;
+    for (const auto& p : plans) {
+        cuda_check(launch_pass(arith, state, static_cast<unsigned char*>(pool_) + p.pool_off, p.desc, stream_),
+                   "launch_pass");
+        bytes += p.bytes;
+    }
+    if (passes_out) *passes_out = plans.size();
+    return bytes;
+}
+
+}  // namespace hqs

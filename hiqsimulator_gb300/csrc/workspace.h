@@ -1,0 +1,85 @@
+// Per-simulator device resources: a CUDA stream, the matrix pool and its
+// pinned staging buffer, reduction scratch, and the fused-pass planner that
+// turns a list of fused gates into sweeps over the state.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <complex>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "hqs_desc.h"
+#include "hqs_kernels.h"
+
+namespace hqs {
+
+using cplx = std::complex<double>;
+
+// One fused gate in state positions.
+struct GateOp {
+    int k = 0;                 // 0..5 targets (0 = scalar factor)
+    bool diag = false;
+    int pos[kMaxK] = {0, 0, 0, 0, 0};  // state position of matrix bit j
+    uint64_t ctrl_mask = 0;    // state positions that must be 1
+    std::vector<cplx> m;       // dense: dim*dim row-major; diag: dim entries; k == 0: 1 entry
+};
+
+struct PassPlan {
+    PassDesc desc;
+    size_t pool_off = 0;       // byte offset of the pass's matrices in the pool
+    uint64_t bytes = 0;        // algorithmic HBM bytes of the sweep
+};
+
+class CudaError : public std::runtime_error {
+public:
+    explicit CudaError(const std::string& m) : std::runtime_error(m) {}
+};
+
+void cuda_check(cudaError_t e, const char* what);
+
+class Workspace {
+public:
+    Workspace();
+    ~Workspace();
+    Workspace(const Workspace&) = delete;
+    Workspace& operator=(const Workspace&) = delete;
+
+    cudaStream_t stream() const { return stream_; }
+    ReduceScratch& reduce() { return rs_; }
+    // Device scratch of at least `bytes` (grown on demand; contents undefined).
+    void* scratch(size_t bytes);
+    // Plan the ops into passes (max_tile_bits, max_ops per pass) and launch
+    // them on the stream. Returns the algorithmic bytes moved.
+    uint64_t apply_ops(void* state, int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits,
+                       int max_ops, uint64_t* passes_out = nullptr);
+    // Upload `bytes` from host memory into a device buffer owned by the
+    // workspace (reused between calls; valid until the next upload).
+    void* upload(const void* host, size_t bytes);
+
+    static size_t mat_elem_bytes(int arith) { return arith == kArithDF ? 16 : (arith == kArithF64 ? 16 : 8); }
+
+private:
+    void ensure_pool(size_t bytes);
+    void ensure_pinned(size_t bytes);
+
+    cudaStream_t stream_ = nullptr;
+    ReduceScratch rs_;
+    void* pool_ = nullptr;
+    size_t pool_bytes_ = 0;
+    void* pinned_ = nullptr;
+    size_t pinned_bytes_ = 0;
+    cudaEvent_t staging_free_ = nullptr;
+    bool staging_pending_ = false;
+    void* scratch_ = nullptr;
+    size_t scratch_bytes_ = 0;
+    void* up_ = nullptr;
+    size_t up_bytes_ = 0;
+};
+
+// Build the pass descriptors for ops (exposed for host-side tests of the planner).
+std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits, int max_ops,
+                                  std::vector<size_t>* op_first = nullptr);
+
+}  // namespace hqs

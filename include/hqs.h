@@ -1,0 +1,202 @@
+/*
+ * hqs.h - C ABI of the GB300 state-vector engine (libhqs.so).
+ *
+ * Drop-in boundary for the C++ engine behind HiQ's SimulatorMPI ProjectQ
+ * backend. The reference binds the engine to Python with pybind11
+ * (_cppsim_mpi.cpp:61-83); this library exposes the same operations as plain
+ * C functions over an opaque handle, and hiqsimulator_gb300/_cppsim_mpi is a
+ * pybind11 module with the reference's class and method names built on top
+ * of it. Every function returns HQS_OK or an error code; the message of the
+ * last error on a handle is hqs_sim_last_error(). Errors that the reference
+ * raises as std::runtime_error (RuntimeError in Python) return
+ * HQS_ERR_RUNTIME with the reference's message.
+ *
+ * Layout: a state of n qubits is 2^n complex amplitudes in position order
+ * (bit p of the index is the qubit at position p), complex128 values as
+ * interleaved (re, im) doubles like std::complex<double>. Matrices are
+ * dim x dim, row-major, interleaved complex128. Bit j of a matrix index acts
+ * on qubit ids[j].
+ *
+ * Threading: a handle is used by one host thread at a time (the reference
+ * runs MPI_THREAD_FUNNELED, SimulatorMPI.cpp:73). Different handles are
+ * independent and may run concurrently; each owns a CUDA stream.
+ */
+#ifndef HQS_H
+#define HQS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HQS_OK 0
+#define HQS_ERR_RUNTIME 1  /* reference std::runtime_error */
+#define HQS_ERR_INVALID 2  /* bad argument (null pointer, short buffer, bad enum) */
+#define HQS_ERR_CUDA 3     /* CUDA failure; message names the call */
+#define HQS_ERR_MEMORY 4   /* host or device allocation failed */
+
+#define HQS_C128 0 /* complex128 state */
+#define HQS_C64 1  /* complex64 state */
+
+#define HQS_ARITH_AUTO 0 /* c128 -> DF, c64 -> F32 */
+#define HQS_ARITH_F64 1  /* native FP64 */
+#define HQS_ARITH_DF 2   /* double-float (2 x FP32), ~48-bit */
+#define HQS_ARITH_F32 3  /* FP32 (complex64 states) */
+
+typedef struct hqs_sim hqs_sim;
+
+/* Message of the last failed call on this thread that had no handle
+ * (hqs_sim_create, kernel-level calls). */
+const char* hqs_last_error(void);
+/* Library version string. */
+const char* hqs_version(void);
+
+/* ------------------------------------------------------------------------
+ * Engine-level API: one entry per method of _cppsim_mpi.SimulatorMPI.
+ * ------------------------------------------------------------------------ */
+
+/* SimulatorMPI(seed, max_local, max_cluster_size): _cppsim_mpi.cpp:64,
+ * SimulatorMPI.cpp:66-104. precision: HQS_C128 / HQS_C64; arith: HQS_ARITH_*. */
+int hqs_sim_create(uint64_t seed, int64_t max_local, int64_t max_cluster_size, int precision, int arith,
+                   hqs_sim** out);
+void hqs_sim_destroy(hqs_sim* sim);
+const char* hqs_sim_last_error(const hqs_sim* sim);
+
+/* allocate_qubit: _cppsim_mpi.cpp:71, SimulatorMPI.cpp:184-216. */
+int hqs_sim_allocate_qubit(hqs_sim* sim, int64_t id);
+/* allocate_qureg(ids, init): _cppsim_mpi.cpp:70, SimulatorMPI.cpp:218-251. */
+int hqs_sim_allocate_qureg(hqs_sim* sim, const int64_t* ids, size_t n, double init_re, double init_im);
+/* deallocate_qubit: _cppsim_mpi.cpp:72, SimulatorMPI.cpp:369-426. */
+int hqs_sim_deallocate_qubit(hqs_sim* sim, int64_t id);
+/* apply_controlled_gate(matrix, ids, ctrls): _cppsim_mpi.cpp:74, SimulatorMPI.cpp:710-815.
+ * m: dim*dim interleaved complex128, row-major; dim == 2^nids. Queues only. */
+int hqs_sim_apply_controlled_gate(hqs_sim* sim, const double* m, size_t dim, const int64_t* ids, size_t nids,
+                                  const int64_t* ctrls, size_t nctrls);
+/* run(): _cppsim_mpi.cpp:78, SimulatorMPI.cpp:441-541. Fuses the queued gates
+ * and schedules the fused gate on the device (asynchronously). */
+int hqs_sim_run(hqs_sim* sim);
+/* measure_qubits(ids): _cppsim_mpi.cpp:73, SimulatorMPI.cpp:897-1008. out[i] = 0/1. */
+int hqs_sim_measure_qubits(hqs_sim* sim, const int64_t* ids, size_t n, uint8_t* out);
+/* get_probability(bits, ids): _cppsim_mpi.cpp:77, SimulatorMPI.cpp:561-600. */
+int hqs_sim_get_probability(hqs_sim* sim, const uint8_t* bits, const int64_t* ids, size_t n, double* out);
+/* get_amplitude(bits, ids): _cppsim_mpi.cpp:76, SimulatorMPI.cpp:602-650. out: (re, im). */
+int hqs_sim_get_amplitude(hqs_sim* sim, const uint8_t* bits, const int64_t* ids, size_t n, double* out);
+/* collapse_wavefunction(ids, values): _cppsim_mpi.cpp:81, SimulatorMPI.cpp:1010-1058. */
+int hqs_sim_collapse_wavefunction(hqs_sim* sim, const int64_t* ids, const uint8_t* values, size_t n);
+/* entropy(): _cppsim_mpi.cpp:79, SimulatorMPI.cpp:681-694. */
+int hqs_sim_entropy(hqs_sim* sim, double* out);
+/* number of allocated qubits (size of the id lists below). */
+int hqs_sim_num_qubits(const hqs_sim* sim, size_t* out);
+/* get_qubits_ids / get_local_qubits_ids / get_global_qubits_ids:
+ * _cppsim_mpi.cpp:65-68, SimulatorMPI.cpp:652-679. out: position order; *n
+ * receives the count (the global list is always empty on one device). */
+int hqs_sim_get_qubits_ids(const hqs_sim* sim, int64_t* out, size_t cap, size_t* n);
+int hqs_sim_get_local_qubits_ids(const hqs_sim* sim, int64_t* out, size_t cap, size_t* n);
+int hqs_sim_get_global_qubits_ids(const hqs_sim* sim, int64_t* out, size_t cap, size_t* n);
+/* set_qubits_perm(ids): _cppsim_mpi.cpp:68, SimulatorMPI.cpp:661-667 (relabels, no data movement). */
+int hqs_sim_set_qubits_perm(hqs_sim* sim, const int64_t* ids, size_t n);
+/* swap_qubits(pairs): _cppsim_mpi.cpp:69, SimulatorMPI.cpp:1060-1138. Pairs are
+ * (global id, local id); one device has no global qubits, so a non-empty list
+ * fails exactly like the reference's lookup. */
+int hqs_sim_swap_qubits(hqs_sim* sim, const int64_t* pairs, size_t n);
+/* cheat_local(): _cppsim_mpi.cpp:80, SimulatorMPI.cpp:543-559. Copies the 2^n
+ * amplitudes (position order, interleaved complex128) into out (cap amplitudes). */
+int hqs_sim_cheat_local(hqs_sim* sim, double* out, size_t cap);
+/* emulate_math: _cppsim_mpi.cpp:75, SimulatorMPI.hpp:218-225: always fails
+ * with "SimulatorMPI::emulate_math() is not supported". */
+int hqs_sim_emulate_math(hqs_sim* sim);
+
+/* Pauli operators, encoded as nterms terms; term t has the factors
+ * [term_off[t], term_off[t+1]) of (qubit index into ids, 'X'|'Y'|'Z') and the
+ * complex coefficient (coefs[2t], coefs[2t+1]). These are the calls the Python
+ * backend makes at hiq/projectq/backends/_sim/_simulator_mpi.py:182-183 and
+ * :222-223 that the reference engine never bound. */
+int hqs_sim_get_expectation_value(hqs_sim* sim, size_t nterms, const size_t* term_off, const int64_t* factor_index,
+                                  const char* factor_pauli, const double* coefs, const int64_t* ids, size_t nids,
+                                  double* out);
+int hqs_sim_apply_qubit_operator(hqs_sim* sim, size_t nterms, const size_t* term_off, const int64_t* factor_index,
+                                 const char* factor_pauli, const double* coefs, const int64_t* ids, size_t nids);
+/* set_wavefunction(wf, ids): called at _simulator_mpi.py:305-306. wf: len
+ * interleaved complex128 amplitudes; ids: every allocated qubit, in the order
+ * the simulator adopts (ids[j] -> position j). */
+int hqs_sim_set_wavefunction(hqs_sim* sim, const double* wf, size_t len, const int64_t* ids, size_t nids);
+
+/* --- extensions (no reference counterpart) --- */
+/* Launch every pending fused gate and wait for the device. */
+int hqs_sim_synchronize(hqs_sim* sim);
+/* shots full-register samples without collapse, one draw each from the
+ * simulator's RNG; out[s] = sampled basis index in position order. */
+int hqs_sim_sample(hqs_sim* sim, uint64_t shots, uint64_t* out);
+/* Move qubits ids[i] to positions[i] with one in-place bit-permutation sweep
+ * (at most 12 positions change). */
+int hqs_sim_move_qubits(hqs_sim* sim, const int64_t* ids, const int* positions, size_t n);
+/* Fused-pass planner limits: tile bits (<= 12), gates per pass (<= 24),
+ * pending fused gates before an automatic launch. 0 keeps a value. */
+int hqs_sim_set_pass_limits(hqs_sim* sim, int max_tile_bits, int max_ops, int defer);
+/* Counters: gates, runs, passes, pass_ops, bytes_moved, flushes. */
+int hqs_sim_stats(const hqs_sim* sim, uint64_t out[6]);
+/* Precision and arithmetic of the handle. */
+int hqs_sim_info(const hqs_sim* sim, int* precision, int* arith);
+/* Device timing on the handle's stream: start records an event after every
+ * pending fused gate is launched; stop records a second one, waits for it and
+ * returns the elapsed milliseconds. */
+int hqs_sim_timer_start(hqs_sim* sim);
+int hqs_sim_timer_stop(hqs_sim* sim, float* ms);
+
+/* Greedy fusion schedule (the rule of HiQ's GreedyScheduler + ClusterScheduler,
+ * hiq/projectq/cengines/_greedyscheduler.py:119-137,
+ * src/scheduler/cluster_scheduler.cpp:41-99): gate g has targets
+ * tgt[toff[g]..toff[g+1]) and controls ctl[coff[g]..coff[g+1]); every gate is
+ * treated as non-diagonal. order[] receives gate indices in emission order and
+ * cluster_end[c] the end of cluster c in order[]; *nclusters the count. */
+int hqs_greedy_schedule(int ngates, const int64_t* tgt, const int* toff, const int64_t* ctl, const int* coff,
+                        int nlocals, const int64_t* locals, int cluster_size, int* order, int* cluster_end,
+                        int* nclusters);
+
+/* ------------------------------------------------------------------------
+ * Kernel-level API on device memory (one fused gate / reduction per call).
+ * state: device pointer to 2^n amplitudes (complex128 for HQS_ARITH_F64/DF,
+ * complex64 for HQS_ARITH_F32). stream: a cudaStream_t or NULL. Calls are
+ * asynchronous except those returning a value to the host.
+ * ------------------------------------------------------------------------ */
+typedef struct hqs_ws hqs_ws;
+int hqs_ws_create(hqs_ws** out);
+void hqs_ws_destroy(hqs_ws* ws);
+/* Apply nops fused gates in order (kernelK / kernelK_diag1 of
+ * src/simulator-mpi/kernels/nointrin/, dispatched as in SimulatorMPI.cpp:470-524).
+ * Gate i: k[i] targets at positions pos[5*i .. 5*i+k[i]) (matrix bit j <->
+ * pos[5*i+j]), control mask ctrl[i], diag[i] != 0 for a diagonal gate. Its
+ * matrix starts at mats (interleaved complex128) after the previous gates':
+ * 4^k entries for a dense gate, 2^k (the diagonal) for a diagonal one, 1 for
+ * k == 0. Gates are grouped into tiled passes of at most max_tile_bits tile
+ * bits and max_ops gates (0 = defaults). *bytes_out (optional) receives the
+ * algorithmic HBM bytes, *passes_out (optional) the number of sweeps. */
+int hqs_apply_gates(hqs_ws* ws, void* state, int n, int arith, int nops, const int* k, const int* pos,
+                    const uint64_t* ctrl, const int* diag, const double* mats, int max_tile_bits, int max_ops,
+                    uint64_t* bytes_out, uint64_t* passes_out);
+/* Sum of |a_i|^2 over (i & mask) == val (getProbability_internal, SimulatorMPI.cpp:841-870). */
+int hqs_probability(hqs_ws* ws, const void* state, int n, int arith, uint64_t mask, uint64_t val, double* out);
+/* nblocks block sums of |a|^2 (calcLocalApproxDistribution before the prefix
+ * sum, SimulatorMPI.cpp:817-839); out: host array of nblocks doubles. */
+int hqs_block_sums(hqs_ws* ws, const void* state, int n, int arith, uint64_t nblocks, double* out);
+/* Zero (i & mask) != val, scale the rest by scale (normalize, SimulatorMPI.cpp:872-895). */
+int hqs_collapse(hqs_ws* ws, void* state, int n, int arith, uint64_t mask, uint64_t val, double scale);
+/* In-place bit permutation: state bit newpos[j] receives old bit oldpos[j] (m <= 12). */
+int hqs_permute_bits(hqs_ws* ws, void* state, int n, int arith, int m, const uint8_t* oldpos, const uint8_t* newpos);
+/* Remove bit pos keeping the half where it equals keep (DeallocateLocalQubit
+ * compaction, SimulatorMPI.cpp:303-318), in place. */
+int hqs_drop_bit(hqs_ws* ws, void* state, int n, int arith, int pos, int keep);
+/* Wait for the workspace's stream. */
+int hqs_ws_synchronize(hqs_ws* ws);
+/* Device timing of the workspace's stream: start records an event; stop
+ * records a second one, waits for it and returns the elapsed milliseconds. */
+int hqs_ws_timer_start(hqs_ws* ws);
+int hqs_ws_timer_stop(hqs_ws* ws, float* ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HQS_H */

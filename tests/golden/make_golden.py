@@ -1,0 +1,185 @@
+"""Generates the golden fixtures in this directory from the reference engine.
+
+Runs the unmodified reference modules built by oracle/build_ref.sh
+(oracle/_ref/_cppsim_mpi, oracle/_ref/_sched_cpp) on seeded circuits from
+hiqsimulator_gb300.circuits and stores what they return:
+
+  ref_states.npz     final states, P(q=1) and measurement outcomes of small
+                     circuits (fusion off and greedy fusion), cheat_local order
+  ref_config0.json   20-qubit config-0 summaries (fusion off / greedy k<=4):
+                     P(q=1) for all 20 qubits, the first 64 amplitudes, the
+                     amplitudes at 64 seeded indices, sum |a|^2
+  ref_sched.json     greedy cluster lists for several circuits
+  ref_rng.json       first uniform draws of std::mt19937(seed) as used by
+                     MeasureQubits (one draw per call, read back via outcomes)
+  ref_errors.json    error messages of the reference for invalid calls
+
+Usage (needs the reference sources and a built oracle/_ref):
+    bash oracle/build_ref.sh && python tests/golden/make_golden.py
+"""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle", "_ref"))
+
+import _cppsim_mpi as REF  # noqa: E402
+import _sched_cpp  # noqa: E402
+
+from hiqsimulator_gb300 import circuits  # noqa: E402
+
+
+def ref_schedule(gates, ctrls, locals_, K):
+    idx = list(range(len(gates)))
+    out = []
+    while True:
+        g = [list(gates[i]) for i in idx]
+        c = [list(ctrls[i]) for i in idx]
+        avail = _sched_cpp.ClusterScheduler(g, c, [False] * len(g), list(locals_), [], K).ScheduleCluster()
+        if not avail:
+            break
+        out.append([idx[i] for i in avail])
+        for i in sorted(avail, reverse=True):
+            del idx[i]
+    return out
+
+
+def run_ref(n, cmds, seed, K):
+    sim = REF.SimulatorMPI(seed, 24, K)
+    sim.allocate_qureg(list(range(n)), 0)
+    circuits.replay(sim, cmds)
+    sim.run()
+    return sim
+
+
+def stream(gates, n, mode, K):
+    if mode == "off":
+        return circuits.fusion_off_stream(gates)
+    G = [list(g.ids) for g in gates]
+    C = [list(g.ctrls) for g in gates]
+    return circuits.greedy_stream(gates, list(range(n)), K, clusters=ref_schedule(G, C, list(range(n)), K))
+
+
+def main():
+    small = {}
+    cases = [("c0_n12_off", 12, 20, "off", 4, 101), ("c0_n12_greedy4", 12, 20, "greedy", 4, 102),
+             ("c0_n14_greedy5", 14, 10, "greedy", 5, 103), ("qft10_greedy5", 10, 0, "qft", 5, 104)]
+    for name, n, layers, mode, K, seed in cases:
+        if mode == "qft":
+            gates = circuits.qft(list(range(n))) + circuits.random_layers(seed, list(range(n)), 2)
+            cmds = stream(gates, n, "greedy", K)
+        else:
+            gates = circuits.random_layers(seed, list(range(n)), layers)
+            cmds = stream(gates, n, mode, K)
+        sim = run_ref(n, cmds, seed, K)
+        id2pos, vec = sim.cheat_local()
+        small[name + "_state"] = np.array(vec, dtype=np.complex128)
+        small[name + "_p1"] = np.array([sim.get_probability([True], [q]) for q in range(n)])
+        small[name + "_meas"] = np.array([int(b) for b in sim.measure_qubits(list(range(n)))], dtype=np.int8)
+        small[name + "_after_meas"] = np.array(sim.cheat_local()[1], dtype=np.complex128)
+    np.savez_compressed(os.path.join(HERE, "ref_states.npz"), **small)
+
+    # 20-qubit config 0 summaries
+    summ = {}
+    n = 20
+    gates = circuits.config0(seed=1234, n=n, layers=20)
+    pick = circuits.rng_for(77).choice(1 << n, size=64, replace=False)
+    for mode in ("off", "greedy"):
+        cmds = stream(gates, n, mode, 4)
+        sim = run_ref(n, cmds, 1234, 4)
+        vec = np.array(sim.cheat_local()[1], dtype=np.complex128)
+        summ[mode] = {
+            "p1": [sim.get_probability([True], [q]) for q in range(n)],
+            "head": [[v.real, v.imag] for v in vec[:64]],
+            "pick_idx": [int(i) for i in pick],
+            "pick": [[vec[i].real, vec[i].imag] for i in pick],
+            "norm": float(np.sum(np.abs(vec) ** 2)),
+            "meas": [int(b) for b in sim.measure_qubits(list(range(n)))],
+        }
+    with open(os.path.join(HERE, "ref_config0.json"), "w") as f:
+        json.dump(summ, f)
+
+    # schedules
+    sch = {}
+    for name, n, layers, K, seed in [("n8_k3", 8, 4, 3, 1), ("n12_k4", 12, 6, 4, 2), ("n20_k4", 20, 3, 4, 3),
+                                     ("n16_k5", 16, 4, 5, 5)]:
+        gates = circuits.random_layers(seed, list(range(n)), layers)
+        sch[name] = {"n": n, "layers": layers, "K": K, "seed": seed,
+                     "clusters": ref_schedule([list(g.ids) for g in gates], [list(g.ctrls) for g in gates],
+                                              list(range(n)), K)}
+    gates = circuits.qft(list(range(10))) + circuits.random_layers(3, list(range(10)), 2)
+    sch["qft10_k5"] = {"clusters": ref_schedule([list(g.ids) for g in gates], [list(g.ctrls) for g in gates],
+                                                list(range(10)), 5)}
+    with open(os.path.join(HERE, "ref_sched.json"), "w") as f:
+        json.dump(sch, f)
+
+    # RNG: with the state |+>^n, measuring all qubits returns the bits of
+    # floor(rnd * 2^n) (up to the block CDF boundaries), so the draws show up
+    # as outcomes; store outcomes of 16 successive measurements for 3 seeds.
+    rng = {}
+    H = circuits.H
+    for seed in (0, 42, 4294967297):
+        sim = REF.SimulatorMPI(seed, 24, 4)
+        n = 16
+        sim.allocate_qureg(list(range(n)), 0)
+        outs = []
+        for _ in range(16):
+            for q in range(n):
+                sim.apply_controlled_gate(H.tolist(), [q], [])
+                sim.run()
+            bits = sim.measure_qubits(list(range(n)))
+            outs.append(sum(int(b) << q for q, b in enumerate(bits)))
+            # return to |0...0>
+            for q in range(n):
+                if bits[q]:
+                    sim.apply_controlled_gate(circuits.X.tolist(), [q], [])
+                    sim.run()
+        rng[str(seed)] = outs
+    with open(os.path.join(HERE, "ref_rng.json"), "w") as f:
+        json.dump(rng, f)
+
+    # error messages
+    errs = {}
+    sim = REF.SimulatorMPI(1, 20, 4)
+    sim.allocate_qureg([0, 1], 0)
+    sim.apply_controlled_gate(H.tolist(), [0], [])
+    sim.run()
+
+    def grab(key, f):
+        try:
+            f()
+            errs[key] = None
+        except Exception as e:  # noqa: BLE001
+            errs[key] = [type(e).__name__, str(e)]
+
+    grab("amp_short", lambda: sim.get_amplitude([True], [0]))
+    grab("amp_not_perm", lambda: sim.get_amplitude([True, False], [0, 0]))
+    grab("prob_unknown", lambda: sim.get_probability([True], [7]))
+    grab("prob_len", lambda: sim.get_probability([True, False], [0]))
+    grab("dealloc_entangled", lambda: sim.deallocate_qubit(0))
+    grab("collapse_zero", lambda: sim.collapse_wavefunction([1], [True]))
+    grab("collapse_len", lambda: sim.collapse_wavefunction([1], [True, False]))
+    grab("emulate_math", lambda: sim.emulate_math(lambda x: x, [[0]], []))
+    grab("swap_pairs", lambda: sim.swap_qubits([0, 1]))
+    grab("dealloc_unknown", lambda: sim.deallocate_qubit(9))
+    grab("measure_unknown", lambda: sim.measure_qubits([5]))
+    sim2 = REF.SimulatorMPI(1, 3, 2)
+    sim2.allocate_qureg([0, 1, 2], 0)
+    grab("alloc_too_many", lambda: sim2.allocate_qubit(3))
+    grab("qureg_init_twice", lambda: sim2.allocate_qureg([5], 0.5))
+    sim3 = REF.SimulatorMPI(1, 20, 4)
+    sim3.allocate_qureg(list(range(6)), 0)
+    sim3.apply_controlled_gate(np.eye(64).tolist(), list(range(6)), [])
+    grab("run_too_big", lambda: sim3.run())
+    with open(os.path.join(HERE, "ref_errors.json"), "w") as f:
+        json.dump(errs, f, indent=1)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,437 @@
+"""Engine-level parity: the drop-in _cppsim_mpi.SimulatorMPI on the GB300
+against the oracle engine and the reference's golden fixtures, plus the
+reference test-suite's known answers (hiq/projectq/backends/_sim/
+_simulator_mpi_test.py) re-expressed as direct API calls."""
+import cmath
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-12
+
+H = [[1 / math.sqrt(2), 1 / math.sqrt(2)], [1 / math.sqrt(2), -1 / math.sqrt(2)]]
+X = [[0, 1], [1, 0]]
+Z = [[1, 0], [0, -1]]
+
+
+def Rx(t):
+    c, s = math.cos(t / 2), math.sin(t / 2)
+    return np.array([[c, -1j * s], [-1j * s, c]])
+
+
+def Ry(t):
+    c, s = math.cos(t / 2), math.sin(t / 2)
+    return np.array([[c, -s], [s, c]], dtype=complex)
+
+
+def Rz(t):
+    return np.array([[cmath.exp(-0.5j * t), 0], [0, cmath.exp(0.5j * t)]])
+
+
+@pytest.fixture(params=["df", "f64"])
+def make(request, hqs, cuda):
+    def f(seed=1, max_local=24, cluster=4):
+        return hqs.SimulatorMPI(seed, max_local, cluster, "c128", request.param)
+    return f
+
+
+def g1(sim, m, q, ctrls=()):
+    sim.apply_controlled_gate(np.asarray(m, dtype=complex).tolist(), [q], list(ctrls))
+
+
+# ------------------------------------------------------------ reference known answers
+
+def test_kqubit_gate_ctrl_mask_path(make):
+    """_simulator_mpi_test.py:247-283: a controlled 4-qubit kron gate (5
+    qubits > cluster 4: the huge-gate control-mask path) undoes Rx/Ry/Rz."""
+    sim = make()
+    m = np.kron(Rz(0.9) @ Ry(-0.1), np.kron(Ry(0.1), np.kron(Rx(0.8), Rx(0.3))))
+    sim.allocate_qureg([0, 1, 2, 3, 4], 0)
+    for q, g in [(0, Rx(-0.3)), (1, Rx(-0.8)), (2, Ry(-0.1)), (3, Rz(-0.9)), (3, Ry(0.1))]:
+        g1(sim, g, q)
+    g1(sim, X, 4)
+    sim.run()
+    sim.apply_controlled_gate(m.tolist(), [0, 1, 2, 3], [4])
+    sim.run()
+    g1(sim, X, 4)
+    sim.run()
+    sim.apply_controlled_gate(m.conj().T.tolist(), [0, 1, 2, 3], [4])
+    sim.run()
+    assert abs(sim.get_amplitude([False] * 5, [4, 0, 1, 2, 3]) - 1.0) < 1e-12
+    sim.apply_controlled_gate(np.eye(64).tolist(), [0, 1, 2, 3, 4, 5], [])
+    with pytest.raises(RuntimeError):
+        sim.run()
+
+
+def test_probability_known_answers(make):
+    """_simulator_mpi_test.py:308-339."""
+    sim = make()
+    q = list(range(6))
+    sim.allocate_qureg(q, 0)
+    for i in q:
+        g1(sim, H, i)
+    sim.run()
+    bits = [0, 0, 1, 0, 1, 0]
+    for i in range(6):
+        assert abs(sim.get_probability([bool(b) for b in bits[:i]], q[:i]) - 0.5 ** i) < 1e-12
+    with pytest.raises(RuntimeError):
+        sim.get_probability([False], [99])
+    for i in q:
+        g1(sim, H, i)
+    g1(sim, Ry(2 * math.acos(math.sqrt(0.3))), 0)
+    sim.run()
+    assert abs(sim.get_probability([False], [0]) - 0.3) < 1e-12
+    g1(sim, Ry(2 * math.acos(math.sqrt(0.4))), 2)
+    sim.run()
+    assert abs(sim.get_probability([False], [2]) - 0.4) < 1e-12
+    assert abs(sim.get_probability([False, False], [0, 2]) - 0.12) < 1e-12
+    assert abs(sim.get_probability([False, True], [0, 2]) - 0.18) < 1e-12
+    assert abs(sim.get_probability([True, False], [0, 2]) - 0.28) < 1e-12
+
+
+def test_amplitude_known_answers(make):
+    """_simulator_mpi_test.py:342-379."""
+    sim = make()
+    q = list(range(6))
+    sim.allocate_qureg(q, 0)
+    for i in q:
+        g1(sim, X, i)
+        g1(sim, H, i)
+    sim.run()
+    assert abs(sim.get_amplitude([False, False, True, False, True, False], q) - 1 / 8) < 1e-12
+    assert abs(sim.get_amplitude([False, False, False, False, True, False], q) + 1 / 8) < 1e-12
+    assert abs(sim.get_amplitude([False, True, True, False, True, False], q) + 1 / 8) < 1e-12
+    for i in q:
+        g1(sim, H, i)
+        g1(sim, X, i)
+    g1(sim, Ry(2 * math.acos(0.3)), 0)
+    sim.run()
+    bits = [False] * 6
+    assert abs(sim.get_amplitude(bits, q) - 0.3) < 1e-12
+    bits[0] = True
+    assert abs(sim.get_amplitude(bits, q) - math.sqrt(0.91)) < 1e-12
+    with pytest.raises(RuntimeError):
+        sim.get_amplitude(bits, q[:-1])
+    with pytest.raises(RuntimeError):
+        sim.get_amplitude(bits, q[:-1] + [q[0]])
+    sim.allocate_qubit(6)
+    with pytest.raises(RuntimeError):
+        sim.get_amplitude(bits, q)
+
+
+def test_collapse_known_answers(make):
+    """_simulator_mpi_test.py:569-603."""
+    sim = make()
+    q = [0, 1, 2, 3]
+    with pytest.raises(RuntimeError):
+        sim.collapse_wavefunction(q, [False] * 4)
+    sim.allocate_qureg(q, 0)
+    sim.collapse_wavefunction(q, [False] * 4)
+    assert abs(sim.get_probability([False] * 4, q) - 1.0) < 1e-12
+    for i in q[1:]:
+        g1(sim, H, i)
+    sim.run()
+    assert abs(sim.get_probability([False] * 4, q) - 0.125) < 1e-12
+    with pytest.raises(RuntimeError):
+        sim.collapse_wavefunction(q, [True, False, False, False])
+    sim.collapse_wavefunction(q[:-1], [False, True, False])
+    assert abs(sim.get_probability([False, True, False, True], q) - 0.5) < 1e-12
+
+
+def test_no_uncompute_exception(make):
+    """_simulator_mpi_test.py:606-614."""
+    sim = make()
+    sim.allocate_qubit(0)
+    g1(sim, H, 0)
+    sim.run()
+    with pytest.raises(RuntimeError):
+        sim.deallocate_qubit(0)
+
+
+def test_functional_entangle(make):
+    """_simulator_mpi_test.py:652-706: GHZ, Toffolis, multi-controlled X."""
+    sim = make()
+    q = list(range(5))
+    sim.allocate_qureg(q, 0)
+    g1(sim, H, 0)
+    for i in q[1:]:
+        g1(sim, X, i, [0])
+    sim.run()
+    _, vec = sim.cheat_local_numpy()
+    assert abs(abs(vec[0]) ** 2 - 0.5) < 1e-12 and abs(abs(vec[31]) ** 2 - 0.5) < 1e-12
+    assert np.max(np.abs(vec[1:31])) < 1e-12
+    for i in q[2:]:
+        g1(sim, X, i, [0])
+    for i in q[2:]:
+        g1(sim, X, i, [0, 1])
+    sim.run()
+    _, vec = sim.cheat_local_numpy()
+    assert abs(abs(vec[0]) ** 2 - 0.5) < 1e-12 and abs(abs(vec[31]) ** 2 - 0.5) < 1e-12
+    g1(sim, X, 4, [0, 1, 2, 3])
+    sim.run()
+    g1(sim, X, 3, [0, 1, 2])
+    sim.run()
+    g1(sim, X, 2, [0, 1])
+    g1(sim, X, 1, [0])
+    g1(sim, H, 0)
+    sim.run()
+    _, vec = sim.cheat_local_numpy()
+    assert abs(abs(vec[0]) ** 2 - 1.0) < 1e-12
+    assert np.max(np.abs(vec[1:])) < 1e-12
+    assert sim.measure_qubits(q) == [False] * 5
+
+
+def test_expectation_known_answers(make):
+    """Commented-out reference test _simulator_mpi_test.py:382-425."""
+    sim = make()
+    q = [0, 1, 2]
+    sim.allocate_qureg(q, 0)
+    sim.run()
+    assert abs(sim.get_expectation_value([([(0, "Z")], 1.0)], q) - 1) < 1e-12
+    g1(sim, X, 0)
+    assert abs(sim.get_expectation_value([([(0, "Z")], 1.0)], q) + 1) < 1e-12
+    g1(sim, H, 0)
+    assert abs(sim.get_expectation_value([([(0, "X")], 1.0)], q) + 1) < 1e-12
+    g1(sim, Z, 0)
+    assert abs(sim.get_expectation_value([([(0, "X")], 1.0)], q) - 1) < 1e-12
+    S = [[1, 0], [0, 1j]]
+    for m in (X, S, Z, X):
+        g1(sim, m, 0)
+    assert abs(sim.get_expectation_value([([(0, "Y")], 1.0)], q) - 1) < 1e-12
+    g1(sim, Z, 0)
+    assert abs(sim.get_expectation_value([([(0, "Y")], 1.0)], q) + 1) < 1e-12
+    op_sum = [([(0, "Y"), (1, "X"), (2, "Z")], 1.0), ([(1, "X")], 1.0)]
+    g1(sim, H, 1)
+    g1(sim, X, 2)
+    assert abs(sim.get_expectation_value(op_sum, q) - 2) < 1e-12
+    g1(sim, X, 2)
+    assert abs(sim.get_expectation_value(op_sum, q) - 0) < 1e-12
+    assert abs(sim.get_expectation_value([([], 0.4)], q) - 0.4) < 1e-12
+    with pytest.raises(RuntimeError):
+        sim.get_expectation_value([([(3, "Z")], 1.0)], q)
+
+
+def test_apply_qubit_operator_known_answers(make):
+    """Commented-out reference test _simulator_mpi_test.py:454-478."""
+    sim = make()
+    q = [0, 1, 2]
+    sim.allocate_qureg(q, 0)
+    sim.run()
+    sim.apply_qubit_operator([([(0, "X"), (1, "Y"), (2, "Z")], 1.0)], q)
+    g1(sim, X, 0)
+    g1(sim, [[0, -1j], [1j, 0]], 1)
+    g1(sim, Z, 2)
+    sim.run()
+    assert abs(sim.get_amplitude([False] * 3, q) - 1.0) < 1e-12
+    g1(sim, H, 0)
+    s = 1 / math.sqrt(2)
+    sim.apply_qubit_operator([([(0, "X")], s), ([(0, "Z")], s)], [0])
+    assert abs(sim.get_amplitude([False] * 3, q) - 1.0) < 1e-12
+    g1(sim, H, 0)
+    sim.apply_qubit_operator([([], 0.5), ([(0, "Z")], 0.5)], [0])
+    assert abs(sim.get_amplitude([False] * 3, q) - s) < 1e-12
+    sim.apply_qubit_operator([([], 0.5), ([(0, "Z")], -0.5)], [0])
+    assert abs(sim.get_amplitude([False] * 3, q)) < 1e-12
+
+
+def test_set_wavefunction_known_answers(make):
+    """Commented-out reference test _simulator_mpi_test.py:540-566."""
+    sim = make()
+    wf = [0.0, 0.0, math.sqrt(0.2), math.sqrt(0.8)]
+    with pytest.raises(RuntimeError):
+        sim.set_wavefunction(wf, [0, 1])
+    sim.allocate_qureg([0, 1], 0)
+    sim.set_wavefunction(wf, [0, 1])
+    assert abs(sim.get_probability([True], [0]) - 0.8) < 1e-12
+    assert abs(sim.get_probability([False, True], [0, 1]) - 0.2) < 1e-12
+    assert abs(sim.get_probability([True], [1]) - 1.0) < 1e-12
+    sim2 = make()
+    sim2.allocate_qubit(0)
+    sim2.set_wavefunction([1.0, 0.0], [0])
+    g1(sim2, [[0, -1j], [1j, 0]], 0)
+    sim2.run()
+    assert abs(sim2.get_amplitude([True], [0]) - 1j) < 1e-12
+
+
+def test_reference_error_messages(make):
+    ref = json.load(open(os.path.join(GOLDEN, "ref_errors.json")))
+    sim = make(1, 20, 4)
+    sim.allocate_qureg([0, 1], 0)
+    g1(sim, H, 0)
+    sim.run()
+    calls = {
+        "amp_short": lambda: sim.get_amplitude([True], [0]),
+        "amp_not_perm": lambda: sim.get_amplitude([True, False], [0, 0]),
+        "prob_unknown": lambda: sim.get_probability([True], [7]),
+        "prob_len": lambda: sim.get_probability([True, False], [0]),
+        "dealloc_entangled": lambda: sim.deallocate_qubit(0),
+        "collapse_zero": lambda: sim.collapse_wavefunction([1], [True]),
+        "collapse_len": lambda: sim.collapse_wavefunction([1], [True, False]),
+        "emulate_math": lambda: sim.emulate_math(lambda x: x, [[0]], []),
+        "swap_pairs": lambda: sim.swap_qubits([0, 1]),
+        "dealloc_unknown": lambda: sim.deallocate_qubit(9),
+        "measure_unknown": lambda: sim.measure_qubits([5]),
+    }
+    for key, f in calls.items():
+        with pytest.raises(RuntimeError) as e:
+            f()
+        assert str(e.value) == ref[key][1], key
+    sim2 = make(1, 3, 2)
+    sim2.allocate_qureg([0, 1, 2], 0)
+    with pytest.raises(RuntimeError) as e:
+        sim2.allocate_qubit(3)
+    assert str(e.value) == ref["alloc_too_many"][1]
+    with pytest.raises(RuntimeError) as e:
+        sim2.allocate_qureg([5], 0.5)
+    assert str(e.value) == ref["qureg_init_twice"][1]
+
+
+# ---------------------------------------------------------- golden fixtures
+
+def _stream(gates, n, mode, K):
+    from hiqsimulator_gb300 import circuits
+    if mode == "off":
+        return circuits.fusion_off_stream(gates)
+    return circuits.greedy_stream(gates, list(range(n)), K)
+
+
+CASES = [("c0_n12_off", 12, 20, "off", 4, 101), ("c0_n12_greedy4", 12, 20, "greedy", 4, 102),
+         ("c0_n14_greedy5", 14, 10, "greedy", 5, 103), ("qft10_greedy5", 10, 0, "qft", 5, 104)]
+
+
+@pytest.mark.parametrize("name,n,layers,mode,K,seed", CASES)
+def test_golden_states(make, name, n, layers, mode, K, seed):
+    from hiqsimulator_gb300 import circuits
+    g = np.load(os.path.join(GOLDEN, "ref_states.npz"))
+    if mode == "qft":
+        gates = circuits.qft(list(range(n))) + circuits.random_layers(seed, list(range(n)), 2)
+        cmds = _stream(gates, n, "greedy", K)
+    else:
+        gates = circuits.random_layers(seed, list(range(n)), layers)
+        cmds = _stream(gates, n, mode, K)
+    sim = make(seed, 24, K)
+    sim.allocate_qureg(list(range(n)), 0)
+    circuits.replay(sim, cmds)
+    sim.run()
+    _, vec = sim.cheat_local_numpy()
+    assert np.max(np.abs(vec - g[name + "_state"])) < TOL
+    p1 = [sim.get_probability([True], [q]) for q in range(n)]
+    assert np.max(np.abs(np.array(p1) - g[name + "_p1"])) < TOL
+    assert [int(b) for b in sim.measure_qubits(list(range(n)))] == list(g[name + "_meas"])
+    _, vec = sim.cheat_local_numpy()
+    assert np.max(np.abs(vec - g[name + "_after_meas"])) < TOL
+
+
+@pytest.mark.parametrize("mode", ["off", "greedy"])
+def test_golden_config0_20q(make, mode):
+    from hiqsimulator_gb300 import circuits
+    ref = json.load(open(os.path.join(GOLDEN, "ref_config0.json")))[mode]
+    n = 20
+    gates = circuits.config0(seed=1234, n=n, layers=20)
+    sim = make(1234, 24, 4)
+    sim.allocate_qureg(list(range(n)), 0)
+    circuits.replay(sim, _stream(gates, n, mode, 4))
+    sim.run()
+    p1 = [sim.get_probability([True], [q]) for q in range(n)]
+    assert np.max(np.abs(np.array(p1) - ref["p1"])) < TOL
+    _, vec = sim.cheat_local_numpy()
+    head = np.array([complex(*v) for v in ref["head"]])
+    assert np.max(np.abs(vec[:64] - head)) < TOL
+    pick = np.array([complex(*v) for v in ref["pick"]])
+    assert np.max(np.abs(vec[ref["pick_idx"]] - pick)) < TOL
+    assert [int(b) for b in sim.measure_qubits(list(range(n)))] == ref["meas"]
+
+
+def test_rng_draws_match_reference(make):
+    ref = json.load(open(os.path.join(GOLDEN, "ref_rng.json")))
+    for seed, outs in ref.items():
+        sim = make(int(seed), 24, 4)
+        n = 16
+        sim.allocate_qureg(list(range(n)), 0)
+        got = []
+        for _ in range(16):
+            for q in range(n):
+                g1(sim, H, q)
+                sim.run()
+            bits = sim.measure_qubits(list(range(n)))
+            got.append(sum(int(b) << q for q, b in enumerate(bits)))
+            for q in range(n):
+                if bits[q]:
+                    g1(sim, X, q)
+                    sim.run()
+        assert got == outs, seed
+
+
+# ------------------------------------------------------ oracle differential
+
+@pytest.mark.parametrize("n,layers,K,seed", [(16, 8, 4, 1), (18, 6, 5, 2), (22, 3, 5, 3)])
+def test_random_circuits_match_oracle(make, n, layers, K, seed):
+    from hiqsimulator_gb300 import circuits
+    from oracle.engine import OracleSimulator
+    qs = list(range(n))
+    gates = circuits.qft(qs) + circuits.random_layers(seed, qs, layers)
+    cmds = circuits.greedy_stream(gates, qs, K)
+    sim = make(seed, 26, K)
+    ref = OracleSimulator(seed, 26, K)
+    for s in (sim, ref):
+        s.allocate_qureg(qs, 0)
+        circuits.replay(s, cmds)
+        s.run()
+    _, vec = sim.cheat_local_numpy()
+    assert np.max(np.abs(vec - ref.vec)) < TOL
+    assert abs(sim.entropy() - ref.entropy()) < 1e-9
+    op = circuits.pauli_sum(seed, n)
+    assert abs(sim.get_expectation_value(op, qs) - ref.get_expectation_value(op, qs)) < 1e-11
+    # deallocate after uncomputing a qubit: drop bit compaction on the device
+    for q in (n - 1, 3, 0):
+        for s in (sim, ref):
+            p1 = s.get_probability([True], [q])
+            s.collapse_wavefunction([q], [p1 > 0.5])
+            s.deallocate_qubit(q)
+    _, vec = sim.cheat_local_numpy()
+    assert np.max(np.abs(vec - ref.vec)) < TOL
+    assert sim.get_qubits_ids() == ref.get_qubits_ids()
+    assert sim.measure_qubits(sim.get_qubits_ids()) == ref.measure_qubits(ref.get_qubits_ids())
+
+
+def test_move_qubits_keeps_every_query(make):
+    from hiqsimulator_gb300 import circuits
+    n = 16
+    qs = list(range(n))
+    gates = circuits.random_layers(5, qs, 3)
+    sim = make(5, 24, 4)
+    sim.allocate_qureg(qs, 0)
+    circuits.replay(sim, circuits.greedy_stream(gates, qs, 4))
+    sim.run()
+    before = [sim.get_probability([True], [q]) for q in qs]
+    amp = sim.get_amplitude([bool((0x5A5A >> q) & 1) for q in qs], qs)
+    sim.move_qubits([15, 14, 13], [0, 1, 2])
+    assert sim.get_qubits_ids()[:3] == [15, 14, 13]
+    after = [sim.get_probability([True], [q]) for q in qs]
+    assert np.max(np.abs(np.array(before) - after)) < 1e-14
+    assert sim.get_amplitude([bool((0x5A5A >> q) & 1) for q in qs], qs) == amp
+
+
+def test_c64_fidelity_against_c128_oracle(hqs, cuda):
+    from hiqsimulator_gb300 import circuits
+    from oracle.engine import OracleSimulator
+    n = 18
+    qs = list(range(n))
+    gates = circuits.brickwork(8, qs, 20)
+    cmds = circuits.greedy_stream(gates, qs, 5)
+    sim = hqs.SimulatorMPI(8, 24, 5, "c64")
+    ref = OracleSimulator(8, 24, 5)
+    for s in (sim, ref):
+        s.allocate_qureg(qs, 0)
+        circuits.replay(s, cmds)
+        s.run()
+    _, vec = sim.cheat_local_numpy()
+    fid = abs(np.vdot(ref.vec, vec)) ** 2
+    assert fid > 1 - 1e-6, fid
+    assert np.max(np.abs(vec - ref.vec)) < 1e-5
