@@ -1,0 +1,331 @@
+#!/usr/bin/env python
+"""Benchmark of the fused-pass hot path on the workload the headline metric
+is quoted on: 30-qubit complex128 state (16 GiB), QFT on all 30 qubits
+followed by 10 seeded random layers (Haar U(2) on every qubit, CNOTs on a
+random perfect matching, one controlled phase), greedy fusion k <= 5.
+
+A step applies the whole fused circuit to the resident state. The metric is
+the reference-equivalent state bandwidth: every fused gate of the greedy
+schedule is one sweep of the reference engine (kernelK, 2 * 2^n * 16 bytes,
+halved per control), so value = sum of those bytes / step time. Inputs are
+larger than L2 (16 GiB state), so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the reference's own CPU algorithm (the oracle port of
+the reference kernels, oracle/, with OpenMP on every host core) on a bounded
+sample of the same workload: the first fused gates of the schedule on the
+30-qubit state.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_QUBITS = 30
+CLUSTER = 5
+SEED = 4321
+METRIC = "30q c128 fused-pass state bandwidth (QFT30 + 10 random layers, greedy fusion k<=5)"
+UNIT = "GB/s"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo", init_method="env://")
+            self.dist = dist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, v):
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+def workload():
+    from hiqsimulator_gb300 import circuits
+    gates = circuits.config1(seed=SEED, n=N_QUBITS, layers=10)
+    t0 = time.time()
+    clusters = circuits.greedy_clusters(gates, list(range(N_QUBITS)), CLUSTER)
+    log("schedule: %d gates -> %d fused gates in %.1fs" % (len(gates), len(clusters), time.time() - t0))
+    cmds = circuits.greedy_stream(gates, list(range(N_QUBITS)), CLUSTER, clusters=clusters)
+    return gates, clusters, cmds
+
+
+def cluster_bytes(gates, clusters, n=N_QUBITS, elem=16):
+    """Reference-equivalent bytes: one read + one write of the state per fused
+    gate; a lone controlled gate too large to fuse touches 2^-c of it."""
+    total = 0
+    for cl in clusters:
+        c = 0
+        if len(cl) == 1:
+            g = gates[cl[0]]
+            if len(g.ids) + len(g.ctrls) > CLUSTER:
+                c = len(g.ctrls)
+        total += 2 * (1 << (n - c)) * elem
+    return total
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=10)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per pass-kernel launch from the committed ncu summary
+    (profiles/pass_kernel_traffic.json), scaled to the 30-qubit state."""
+    p = os.path.join(ROOT, "profiles", "pass_kernel_traffic.json")
+    if not os.path.exists(p):
+        return None
+    d = json.load(open(p))
+    return float(d["bytes_per_amplitude"]) * (1 << N_QUBITS)
+
+
+def cpu_sample(cmds, clusters, max_gates, budget_s):
+    """The oracle port of the reference engine on the host cores: the first
+    fused gates of the schedule on a fresh 30-qubit state. Returns
+    (GB/s, threads, description)."""
+    from oracle.engine import OracleSimulator
+    sim = OracleSimulator(SEED, N_QUBITS, CLUSTER)
+    sim.allocate_qureg(list(range(N_QUBITS)), 0)
+    # one run() per cluster; time only the sweeps (fusion happens in run())
+    done = 0
+    t_total = 0.0
+    it = iter(cmds)
+    for c in it:
+        if c[0] == "gate":
+            g = c[1]
+            sim.apply_controlled_gate(g.matrix.tolist(), list(g.ids), list(g.ctrls))
+            continue
+        t0 = time.perf_counter()
+        sim.run()
+        t_total += time.perf_counter() - t0
+        done += 1
+        if done >= max_gates or t_total > budget_s:
+            break
+    byts = done * 2 * (1 << N_QUBITS) * 16
+    threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    return byts / t_total / 1e9, threads, "%d fused gates of the schedule on the 30-qubit state (%.1f s)" % (
+        done, t_total)
+
+
+def run_reference(args, dist):
+    if dist.rank != 0:
+        return 0
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    os.environ.setdefault("OMP_PROC_BIND", "spread")
+    _, clusters, cmds = workload()
+    vals = []
+    for s in range(args.warmup + args.steps):
+        v, threads, desc = cpu_sample(cmds, clusters, max_gates=2, budget_s=20.0)
+        if s >= args.warmup:
+            vals.append(v)
+        log("reference step %d: %.2f GB/s (%s)" % (s, v, desc))
+    value = statistics.median(vals)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded circuits)",
+            "config": {"workload": "QFT30 + 10 random layers, greedy fusion k<=5, complex128, 30 qubits",
+                       "sample": desc},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, dist):
+    import hiqsimulator_gb300 as hqs
+    from hiqsimulator_gb300 import circuits
+    gates, clusters, cmds = workload()
+    ref_bytes = cluster_bytes(gates, clusters)
+    zz, shots = circuits.config1_observables(SEED, N_QUBITS)
+    ids = list(range(N_QUBITS))
+
+    # ---- device-resident timing (value): state allocated once, steps replay the
+    # fused circuit through the engine; CUDA events on the engine's stream.
+    sim = hqs.SimulatorMPI(SEED, N_QUBITS, CLUSTER, "c128", args.arith)
+    sim.set_pass_limits(defer=args.defer)
+    sim.allocate_qureg(ids, 0)
+    sim.synchronize()
+    for _ in range(args.warmup):
+        circuits.replay(sim, cmds)
+        sim.synchronize()
+    clocks = ClockSampler(dist.local)
+    dist.barrier()
+    clocks.start()
+    s0 = sim.stats()
+    sim.enable_pass_timing(True)
+    sim.timer_start()
+    for _ in range(args.steps):
+        circuits.replay(sim, cmds)
+    ms = sim.timer_stop()
+    pt = sim.pass_timing()
+    sim.enable_pass_timing(False)
+    clk = clocks.stop()
+    s1 = sim.stats()
+    ms = dist.max(ms)
+    dist.barrier()
+    launches = s1["passes"] - s0["passes"]
+    value = dist.ws * args.steps * ref_bytes / (ms / 1e3) / 1e9
+    log("value: %.1f GB/s over %d steps (%.1f ms/step, %d launches)" % (value, args.steps, ms / args.steps, launches))
+
+    # roofline of the dominant kernel (the fused pass): bytes it moved / its time
+    peak, peak_kind = measured_peak()
+    achieved = pt["bytes"] / (pt["ms"] / 1e3) / 1e9 if pt["ms"] > 0 else 0.0
+    traffic = profile_traffic()
+    per_launch_bytes = pt["bytes"] / max(pt["launches"], 1)
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic, "peak_source": peak_kind, "kernel": "pass_kernel<%s>" % sim.arith,
+            "launches": pt["launches"], "algorithmic_bytes_per_launch": per_launch_bytes,
+            "avg_launch_ms": pt["ms"] / max(pt["launches"], 1)}
+    del sim
+
+    # ---- end to end through the drop-in API: fresh simulator, allocate, gates
+    # from host lists, <Z_i Z_j> for 64 pairs and 1024 samples back to the host.
+    def e2e_step():
+        s = hqs.SimulatorMPI(SEED, N_QUBITS, CLUSTER, "c128", args.arith)
+        s.set_pass_limits(defer=args.defer)
+        s.allocate_qureg(ids, 0)
+        circuits.replay(s, cmds)
+        s.run()
+        ev = [s.get_expectation_value([([(a, "Z"), (b, "Z")], 1.0)], ids) for a, b in zz]
+        smp = s.sample(shots)
+        return ev, smp
+
+    e2e_steps = max(1, min(args.steps, 3))
+    e2e_step()
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = dist.max(time.perf_counter() - t0)
+    h2d = sum(16 * len(c[1].matrix) ** 2 for c in cmds if c[0] == "gate")
+    d2h = 8 * len(zz) + 8 * shots
+    e2e = {"value": dist.ws * e2e_steps * ref_bytes / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s / e2e_steps}
+
+    cpu = None
+    if dist.rank == 0 and not args.no_cpu_baseline:
+        os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+        v, threads, desc = cpu_sample(cmds, clusters, max_gates=2, budget_s=20.0)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
+
+    if dist.rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "c128 (%s arithmetic)" % args.arith,
+                "data": "synthetic (seeded circuits)",
+                "config": {"workload": "QFT30 + 10 random layers, greedy fusion k<=5, complex128, 30 qubits",
+                           "fused_gates_per_step": len(clusters), "gates_per_step": len(gates),
+                           "state_bytes": 16 << N_QUBITS, "l2": "inputs larger than L2 (16 GiB state)",
+                           "parallelism": "replicas" if dist.ws > 1 else "single GPU"},
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--arith", default="df", choices=["df", "f64"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--defer", type=int, default=8, help="fused gates queued before the engine launches")
+    args = ap.parse_args()
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            return run_reference(args, dist)
+        return run_ours(args, dist)
+    finally:
+        dist.close()
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -156,32 +156,35 @@ int hqs_sim_measure_qubits(hqs_sim* sim, const int64_t* ids, size_t n, uint8_t* 
     });
 }
 
-int hqs_sim_get_probability(hqs_sim* sim, const uint8_t* bits, const int64_t* ids, size_t n, double* out) {
+int hqs_sim_get_probability(hqs_sim* sim, const uint8_t* bits, size_t nbits, const int64_t* ids, size_t nids,
+                            double* out) {
     SIM_CALL(sim, {
-        need(out && (n == 0 || (ids && bits)), "null arrays");
-        std::vector<bool> b(n);
-        for (size_t i = 0; i < n; ++i) b[i] = bits[i] != 0;
-        *out = sim->eng->get_probability(b, std::vector<int64_t>(ids, ids + n));
+        need(out && (nids == 0 || ids) && (nbits == 0 || bits), "null arrays");
+        std::vector<bool> b(nbits);
+        for (size_t i = 0; i < nbits; ++i) b[i] = bits[i] != 0;
+        *out = sim->eng->get_probability(b, std::vector<int64_t>(ids, ids + nids));
     });
 }
 
-int hqs_sim_get_amplitude(hqs_sim* sim, const uint8_t* bits, const int64_t* ids, size_t n, double* out) {
+int hqs_sim_get_amplitude(hqs_sim* sim, const uint8_t* bits, size_t nbits, const int64_t* ids, size_t nids,
+                          double* out) {
     SIM_CALL(sim, {
-        need(out && (n == 0 || (ids && bits)), "null arrays");
-        std::vector<bool> b(n);
-        for (size_t i = 0; i < n; ++i) b[i] = bits[i] != 0;
-        const hqs::cplx a = sim->eng->get_amplitude(b, std::vector<int64_t>(ids, ids + n));
+        need(out && (nids == 0 || ids) && (nbits == 0 || bits), "null arrays");
+        std::vector<bool> b(nbits);
+        for (size_t i = 0; i < nbits; ++i) b[i] = bits[i] != 0;
+        const hqs::cplx a = sim->eng->get_amplitude(b, std::vector<int64_t>(ids, ids + nids));
         out[0] = a.real();
         out[1] = a.imag();
     });
 }
 
-int hqs_sim_collapse_wavefunction(hqs_sim* sim, const int64_t* ids, const uint8_t* values, size_t n) {
+int hqs_sim_collapse_wavefunction(hqs_sim* sim, const int64_t* ids, size_t nids, const uint8_t* values,
+                                  size_t nvalues) {
     SIM_CALL(sim, {
-        need(n == 0 || (ids && values), "null arrays");
-        std::vector<bool> v(n);
-        for (size_t i = 0; i < n; ++i) v[i] = values[i] != 0;
-        sim->eng->collapse_wavefunction(std::vector<int64_t>(ids, ids + n), v);
+        need((nids == 0 || ids) && (nvalues == 0 || values), "null arrays");
+        std::vector<bool> v(nvalues);
+        for (size_t i = 0; i < nvalues; ++i) v[i] = values[i] != 0;
+        sim->eng->collapse_wavefunction(std::vector<int64_t>(ids, ids + nids), v);
     });
 }
 
@@ -325,6 +328,23 @@ int hqs_sim_timer_stop(hqs_sim* sim, float* ms) {
         hqs::cuda_check(cudaEventRecord(sim->t1, sim->eng->stream()), "cudaEventRecord");
         hqs::cuda_check(cudaEventSynchronize(sim->t1), "cudaEventSynchronize");
         hqs::cuda_check(cudaEventElapsedTime(ms, sim->t0, sim->t1), "cudaEventElapsedTime");
+    });
+}
+
+int hqs_sim_set_pass_timing(hqs_sim* sim, int on) {
+    SIM_CALL(sim, {
+        sim->eng->flush();
+        sim->eng->workspace().set_timing(on != 0);
+    });
+}
+
+int hqs_sim_pass_timing(hqs_sim* sim, uint64_t* launches, uint64_t* bytes, double* ms) {
+    SIM_CALL(sim, {
+        sim->eng->flush();
+        const hqs::Workspace::PassTiming t = sim->eng->workspace().collect_timing();
+        if (launches) *launches = t.launches;
+        if (bytes) *bytes = t.bytes;
+        if (ms) *ms = t.ms;
     });
 }
 

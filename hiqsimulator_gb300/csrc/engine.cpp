@@ -522,11 +522,13 @@ void Engine::apply_qubit_operator(const std::vector<PauliTerm>& terms, const std
         return;
     }
     const size_t melem = Workspace::mat_elem_bytes(arith_);
-    std::vector<unsigned char> blob(T * 3 * 8 + 2 * T * melem);
+    // coefficient table starts on a 256-byte boundary (16-byte vector loads)
+    const size_t coff = (T * 3 * 8 + 255) & ~(size_t)255;
+    std::vector<unsigned char> blob(coff + 2 * T * melem);
     std::memcpy(blob.data(), xm.data(), T * 8);
     std::memcpy(blob.data() + T * 8, ym.data(), T * 8);
     std::memcpy(blob.data() + 2 * T * 8, zm.data(), T * 8);
-    unsigned char* cb = blob.data() + 3 * T * 8;
+    unsigned char* cb = blob.data() + coff;
     for (size_t t = 0; t < T; ++t) {
         cplx c = terms[t].coef;
         const int ny = __builtin_popcountll(ym[t]) & 3;
@@ -561,7 +563,7 @@ void Engine::apply_qubit_operator(const std::vector<PauliTerm>& terms, const std
     }
     const unsigned char* d = static_cast<const unsigned char*>(ws_.upload(blob.data(), blob.size()));
     cuda_check(pauli_apply(arith_, state_, spare_, n(), (int)T, (const uint64_t*)d, (const uint64_t*)(d + T * 8),
-                           (const uint64_t*)(d + 2 * T * 8), (const double*)(d + 3 * T * 8), ws_.stream()),
+                           (const uint64_t*)(d + 2 * T * 8), (const double*)(d + coff), ws_.stream()),
                "pauli_apply");
     std::swap(state_, spare_);
 }

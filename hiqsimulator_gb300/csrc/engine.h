@@ -90,6 +90,7 @@ public:
     // Fused-pass planner knobs.
     void set_pass_limits(int max_tile_bits, int max_ops, int defer);
     void* device_state() { return state_; }
+    Workspace& workspace() { return ws_; }
     cudaStream_t stream() const { return ws_.stream(); }
 
 private:

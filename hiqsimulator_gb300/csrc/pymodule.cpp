@@ -141,13 +141,13 @@ public:
     cplx get_amplitude(const std::vector<bool>& bits, const Ids& ids) {
         std::vector<uint8_t> b(bits.begin(), bits.end());
         double out[2];
-        check(hqs_sim_get_amplitude(h_, b.data(), ids.data(), ids.size(), out));
+        check(hqs_sim_get_amplitude(h_, b.data(), b.size(), ids.data(), ids.size(), out));
         return cplx(out[0], out[1]);
     }
     double get_probability(const std::vector<bool>& bits, const Ids& ids) {
         std::vector<uint8_t> b(bits.begin(), bits.end());
         double out = 0;
-        check(hqs_sim_get_probability(h_, b.data(), ids.data(), ids.size(), &out));
+        check(hqs_sim_get_probability(h_, b.data(), b.size(), ids.data(), ids.size(), &out));
         return out;
     }
     void run() { check(hqs_sim_run(h_)); }
@@ -179,7 +179,7 @@ public:
     }
     void collapse_wavefunction(const Ids& ids, const std::vector<bool>& values) {
         std::vector<uint8_t> v(values.begin(), values.end());
-        check(hqs_sim_collapse_wavefunction(h_, ids.data(), v.data(), ids.size()));
+        check(hqs_sim_collapse_wavefunction(h_, ids.data(), ids.size(), v.data(), v.size()));
     }
     double get_expectation_value(const py::object& op, const Ids& ids) {
         const PauliArgs a = encode(op);
@@ -233,6 +233,17 @@ public:
         check(hqs_sim_info(h_, &p, &a));
         return a == HQS_ARITH_F64 ? "f64" : (a == HQS_ARITH_DF ? "df" : "f32");
     }
+    void enable_pass_timing(bool on) { check(hqs_sim_set_pass_timing(h_, on ? 1 : 0)); }
+    py::dict pass_timing() {
+        uint64_t launches = 0, bytes = 0;
+        double ms = 0;
+        check(hqs_sim_pass_timing(h_, &launches, &bytes, &ms));
+        py::dict d;
+        d["launches"] = launches;
+        d["bytes"] = bytes;
+        d["ms"] = ms;
+        return d;
+    }
     void timer_start() { check(hqs_sim_timer_start(h_)); }
     float timer_stop() {
         float ms = 0;
@@ -279,6 +290,8 @@ PYBIND11_MODULE(_cppsim_mpi, m) {
         .def("set_pass_limits", &SimulatorMPI::set_pass_limits, py::arg("max_tile_bits") = 0, py::arg("max_ops") = 0,
              py::arg("defer") = 0)
         .def("stats", &SimulatorMPI::stats)
+        .def("enable_pass_timing", &SimulatorMPI::enable_pass_timing)
+        .def("pass_timing", &SimulatorMPI::pass_timing)
         .def("timer_start", &SimulatorMPI::timer_start)
         .def("timer_stop", &SimulatorMPI::timer_stop)
         .def_property_readonly("precision", &SimulatorMPI::precision)

@@ -28,6 +28,11 @@ Workspace::~Workspace() {
     cudaFree(scratch_);
     cudaFree(up_);
     if (staging_free_) cudaEventDestroy(staging_free_);
+    for (auto& t : timed_) {
+        cudaEventDestroy(t.a);
+        cudaEventDestroy(t.b);
+    }
+    for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -215,12 +220,49 @@ uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<G
     staging_pending_ = true;
     uint64_t bytes = 0;
     for (const auto& p : plans) {
+        TimedLaunch tl{nullptr, nullptr, p.bytes};
+        if (timing_) {
+            tl.a = take_event();
+            tl.b = take_event();
+            cuda_check(cudaEventRecord(tl.a, stream_), "cudaEventRecord");
+        }
         cuda_check(launch_pass(arith, state, static_cast<unsigned char*>(pool_) + p.pool_off, p.desc, stream_),
                    "launch_pass");
+        if (timing_) {
+            cuda_check(cudaEventRecord(tl.b, stream_), "cudaEventRecord");
+            timed_.push_back(tl);
+        }
         bytes += p.bytes;
     }
     if (passes_out) *passes_out = plans.size();
     return bytes;
+}
+
+cudaEvent_t Workspace::take_event() {
+    if (!event_pool_.empty()) {
+        cudaEvent_t e = event_pool_.back();
+        event_pool_.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cuda_check(cudaEventCreate(&e), "cudaEventCreate");
+    return e;
+}
+
+Workspace::PassTiming Workspace::collect_timing() {
+    PassTiming t;
+    for (auto& tl : timed_) {
+        cuda_check(cudaEventSynchronize(tl.b), "cudaEventSynchronize");
+        float ms = 0.f;
+        cuda_check(cudaEventElapsedTime(&ms, tl.a, tl.b), "cudaEventElapsedTime");
+        t.ms += ms;
+        t.bytes += tl.bytes;
+        ++t.launches;
+        event_pool_.push_back(tl.a);
+        event_pool_.push_back(tl.b);
+    }
+    timed_.clear();
+    return t;
 }
 
 }  // namespace hqs

@@ -60,6 +60,17 @@ public:
 
     static size_t mat_elem_bytes(int arith) { return arith == kArithDF ? 16 : (arith == kArithF64 ? 16 : 8); }
 
+    // Per-launch device timing of the apply passes (CUDA events around each
+    // launch on the workspace stream). collect_timing() waits for the events,
+    // returns the totals since the last collection and clears them.
+    struct PassTiming {
+        uint64_t launches = 0;
+        uint64_t bytes = 0;
+        double ms = 0.0;
+    };
+    void set_timing(bool on) { timing_ = on; }
+    PassTiming collect_timing();
+
 private:
     void ensure_pool(size_t bytes);
     void ensure_pinned(size_t bytes);
@@ -76,6 +87,14 @@ private:
     size_t scratch_bytes_ = 0;
     void* up_ = nullptr;
     size_t up_bytes_ = 0;
+    bool timing_ = false;
+    struct TimedLaunch {
+        cudaEvent_t a, b;
+        uint64_t bytes;
+    };
+    std::vector<TimedLaunch> timed_;
+    std::vector<cudaEvent_t> event_pool_;
+    cudaEvent_t take_event();
 };
 
 // Build the pass descriptors for ops (exposed for host-side tests of the planner).

@@ -80,11 +80,14 @@ int hqs_sim_run(hqs_sim* sim);
 /* measure_qubits(ids): _cppsim_mpi.cpp:73, SimulatorMPI.cpp:897-1008. out[i] = 0/1. */
 int hqs_sim_measure_qubits(hqs_sim* sim, const int64_t* ids, size_t n, uint8_t* out);
 /* get_probability(bits, ids): _cppsim_mpi.cpp:77, SimulatorMPI.cpp:561-600. */
-int hqs_sim_get_probability(hqs_sim* sim, const uint8_t* bits, const int64_t* ids, size_t n, double* out);
+int hqs_sim_get_probability(hqs_sim* sim, const uint8_t* bits, size_t nbits, const int64_t* ids, size_t nids,
+                            double* out);
 /* get_amplitude(bits, ids): _cppsim_mpi.cpp:76, SimulatorMPI.cpp:602-650. out: (re, im). */
-int hqs_sim_get_amplitude(hqs_sim* sim, const uint8_t* bits, const int64_t* ids, size_t n, double* out);
+int hqs_sim_get_amplitude(hqs_sim* sim, const uint8_t* bits, size_t nbits, const int64_t* ids, size_t nids,
+                          double* out);
 /* collapse_wavefunction(ids, values): _cppsim_mpi.cpp:81, SimulatorMPI.cpp:1010-1058. */
-int hqs_sim_collapse_wavefunction(hqs_sim* sim, const int64_t* ids, const uint8_t* values, size_t n);
+int hqs_sim_collapse_wavefunction(hqs_sim* sim, const int64_t* ids, size_t nids, const uint8_t* values,
+                                  size_t nvalues);
 /* entropy(): _cppsim_mpi.cpp:79, SimulatorMPI.cpp:681-694. */
 int hqs_sim_entropy(hqs_sim* sim, double* out);
 /* number of allocated qubits (size of the id lists below). */
@@ -144,6 +147,12 @@ int hqs_sim_info(const hqs_sim* sim, int* precision, int* arith);
  * returns the elapsed milliseconds. */
 int hqs_sim_timer_start(hqs_sim* sim);
 int hqs_sim_timer_stop(hqs_sim* sim, float* ms);
+/* Per-launch timing of the apply passes: while on, CUDA events bracket every
+ * pass launch; hqs_sim_pass_timing waits for them and returns the number of
+ * launches, their algorithmic HBM bytes and summed device milliseconds since
+ * the previous call. */
+int hqs_sim_set_pass_timing(hqs_sim* sim, int on);
+int hqs_sim_pass_timing(hqs_sim* sim, uint64_t* launches, uint64_t* bytes, double* ms);
 
 /* Greedy fusion schedule (the rule of HiQ's GreedyScheduler + ClusterScheduler,
  * hiq/projectq/cengines/_greedyscheduler.py:119-137,

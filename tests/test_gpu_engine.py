@@ -42,7 +42,9 @@ def make(request, hqs, cuda):
 
 
 def g1(sim, m, q, ctrls=()):
+    """One gate followed by run() (the backend's gate_fusion=False protocol)."""
     sim.apply_controlled_gate(np.asarray(m, dtype=complex).tolist(), [q], list(ctrls))
+    sim.run()
 
 
 # ------------------------------------------------------------ reference known answers
