@@ -19,7 +19,7 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["kernels.cu"]
+CU_SOURCES = ["kernels.cu", "noalloc.cu"]
 CXX_SOURCES = ["fusion.cpp", "workspace.cpp", "engine.cpp", "scheduler.cpp", "capi.cpp"]
 HEADERS = ["hqs_desc.h", "hqs_kernels.h", "hqs_arith.cuh", "fusion.h", "workspace.h", "engine.h"]
 

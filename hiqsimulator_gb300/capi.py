@@ -83,6 +83,7 @@ def load():
     lib.hqs_collapse.argtypes = [_vp, _vp, _i, _i, _u64, _u64, _d]
     lib.hqs_permute_bits.argtypes = [_vp, _vp, _i, _i, _i, _P(ctypes.c_uint8), _P(ctypes.c_uint8)]
     lib.hqs_drop_bit.argtypes = [_vp, _vp, _i, _i, _i, _i]
+    lib.hqs_probability_noalloc.argtypes = [_vp, _i, _i, _u64, _u64, _vp, _vp]
     lib.hqs_ws_synchronize.argtypes = [_vp]
     lib.hqs_ws_timer_start.argtypes = [_vp]
     lib.hqs_ws_timer_stop.argtypes = [_vp, _P(ctypes.c_float)]

@@ -12,6 +12,7 @@
 #include "workspace.h"
 
 namespace hqs {
+void set_last_error(const std::string& msg);
 int greedy_schedule(int ngates, const int64_t* tgt, const int* toff, const int64_t* ctl, const int* coff, int nlocals,
                     const int64_t* locals, int K, int* order, int* cluster_end);
 }
@@ -30,6 +31,14 @@ struct hqs_ws {
 namespace {
 
 thread_local std::string g_err;
+
+}  // namespace
+
+namespace hqs {
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace hqs
+
+namespace {
 
 template <class F>
 int guarded(std::string& err, F&& f) {

@@ -197,6 +197,19 @@ int hqs_permute_bits(hqs_ws* ws, void* state, int n, int arith, int m, const uin
 /* Remove bit pos keeping the half where it equals keep (DeallocateLocalQubit
  * compaction, SimulatorMPI.cpp:303-318), in place. */
 int hqs_drop_bit(hqs_ws* ws, void* state, int n, int arith, int pos, int keep);
+/* Probability sum for callers that cannot allocate device memory (no
+ * counterpart in the reference). Same result as hqs_probability, but every
+ * scratch byte lives in a fixed 32 KiB __device__ array inside libhqs.so and
+ * the sum is written to the caller's device pointer d_out on `stream` (a
+ * cudaStream_t, NULL for the legacy default stream), asynchronously; nothing
+ * is allocated, freed or synchronized. For code that runs under a foreign
+ * memory pool or inside recorded launch sequences, where cudaMalloc is not
+ * allowed. Limit: at most 2^32 amplitudes matching (mask, val) per call;
+ * larger requests fail with HQS_ERR_INVALID. All calls on a device share the
+ * array, so calls that overlap on the GPU race; the first call on a device
+ * looks the array up and should come before any stream capture. */
+int hqs_probability_noalloc(const void* state, int n, int arith, uint64_t mask, uint64_t val, double* d_out,
+                            void* stream);
 /* Wait for the workspace's stream. */
 int hqs_ws_synchronize(hqs_ws* ws);
 /* Device timing of the workspace's stream: start records an event; stop
