@@ -31,7 +31,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N_QUBITS = 30
+N_QUBITS = 30  # overridden by --qubits for profiling runs on smaller states
 CLUSTER = 5
 SEED = 4321
 METRIC = "30q c128 fused-pass state bandwidth (QFT30 + 10 random layers, greedy fusion k<=5)"
@@ -85,9 +85,10 @@ def workload():
     return gates, clusters, cmds
 
 
-def cluster_bytes(gates, clusters, n=N_QUBITS, elem=16):
+def cluster_bytes(gates, clusters, n=None, elem=16):
     """Reference-equivalent bytes: one read + one write of the state per fused
     gate; a lone controlled gate too large to fuse touches 2^-c of it."""
+    n = N_QUBITS if n is None else n
     total = 0
     for cl in clusters:
         c = 0
@@ -275,17 +276,19 @@ def run_ours(args, dist):
         smp = s.sample(shots)
         return ev, smp
 
-    e2e_steps = max(1, min(args.steps, 3))
-    e2e_step()
-    dist.barrier()
-    t0 = time.perf_counter()
-    for _ in range(e2e_steps):
+    e2e = None
+    if not args.no_e2e:
+        e2e_steps = max(1, min(args.steps, 3))
         e2e_step()
-    e2e_s = dist.max(time.perf_counter() - t0)
-    h2d = sum(16 * len(c[1].matrix) ** 2 for c in cmds if c[0] == "gate")
-    d2h = 8 * len(zz) + 8 * shots
-    e2e = {"value": dist.ws * e2e_steps * ref_bytes / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s / e2e_steps}
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            e2e_step()
+        e2e_s = dist.max(time.perf_counter() - t0)
+        h2d = sum(16 * len(c[1].matrix) ** 2 for c in cmds if c[0] == "gate")
+        d2h = 8 * len(zz) + 8 * shots
+        e2e = {"value": dist.ws * e2e_steps * ref_bytes / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "seconds_per_step": e2e_s / e2e_steps}
 
     cpu = None
     if dist.rank == 0 and not args.no_cpu_baseline:
@@ -298,7 +301,8 @@ def run_ours(args, dist):
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "c128 (%s arithmetic)" % args.arith,
                 "data": "synthetic (seeded circuits)",
-                "config": {"workload": "QFT30 + 10 random layers, greedy fusion k<=5, complex128, 30 qubits",
+                "config": {"workload": "QFT%d + 10 random layers, greedy fusion k<=5, complex128, %d qubits" % (
+                               N_QUBITS, N_QUBITS),
                            "fused_gates_per_step": len(clusters), "gates_per_step": len(gates),
                            "state_bytes": 16 << N_QUBITS, "l2": "inputs larger than L2 (16 GiB state)",
                            "parallelism": "replicas" if dist.ws > 1 else "single GPU"},
@@ -317,7 +321,11 @@ def main():
     ap.add_argument("--arith", default="df", choices=["df", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--defer", type=int, default=8, help="fused gates queued before the engine launches")
+    ap.add_argument("--qubits", type=int, default=30, help="state size (30 is the benchmark configuration)")
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
+    global N_QUBITS
+    N_QUBITS = args.qubits
     dist = Dist()
     try:
         if args.impl == "reference":
