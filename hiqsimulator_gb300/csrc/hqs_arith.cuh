@@ -93,72 +93,80 @@ __device__ __forceinline__ void df_norm(float& h, float& l) {
 }
 
 // ------------------------------------------------------------------- policies
+// store_t: element of the state in HBM. comp_t: element of a tile in shared
+// memory (converted once when a tile is loaded and once when it is stored).
+// mat_t: matrix element in the pass's matrix pool.
 struct ArithF64 {
     using store_t = double2;
+    using comp_t = double2;
     using mat_t = double2;
-    struct xval { double re, im; };
     struct acc_t { double re, im; };
     static constexpr int kId = 1;
-    __device__ __forceinline__ static xval load(const store_t v) { return {v.x, v.y}; }
+    __device__ __forceinline__ static comp_t to_comp(const store_t v) { return v; }
+    __device__ __forceinline__ static store_t from_comp(const comp_t v) { return v; }
     __device__ __forceinline__ static void zero(acc_t& a) { a.re = 0.0; a.im = 0.0; }
-    __device__ __forceinline__ static void mac(acc_t& a, const mat_t m, const xval& x) {
-        a.re = fma(m.x, x.re, a.re);
-        a.re = fma(-m.y, x.im, a.re);
-        a.im = fma(m.x, x.im, a.im);
-        a.im = fma(m.y, x.re, a.im);
+    __device__ __forceinline__ static void mac(acc_t& a, const mat_t m, const comp_t x) {
+        a.re = fma(m.x, x.x, a.re);
+        a.re = fma(-m.y, x.y, a.re);
+        a.im = fma(m.x, x.y, a.im);
+        a.im = fma(m.y, x.x, a.im);
     }
-    __device__ __forceinline__ static store_t finish(acc_t& a) { return make_double2(a.re, a.im); }
-    __device__ __forceinline__ static store_t mul(const mat_t m, const store_t v) {
+    __device__ __forceinline__ static comp_t finish(acc_t& a) { return make_double2(a.re, a.im); }
+    __device__ __forceinline__ static comp_t mul(const mat_t m, const comp_t v) {
         return make_double2(fma(m.x, v.x, -m.y * v.y), fma(m.x, v.y, m.y * v.x));
     }
 };
 
 struct ArithDF {
     using store_t = double2;
-    using mat_t = float4;  // (hi.re, hi.im, lo.re, lo.im)
-    struct xval { float hr, hi, lr, li; };
+    using comp_t = float4;  // (hi.re, hi.im, lo.re, lo.im)
+    using mat_t = float4;   // (hi.re, hi.im, lo.re, lo.im)
     struct acc_t { float rh, rl, ih, il; };
     static constexpr int kId = 2;
-    __device__ __forceinline__ static xval load(const store_t v) {
+    __device__ __forceinline__ static comp_t to_comp(const store_t v) {
         const DF a = df_split(v.x), b = df_split(v.y);
-        return {a.h, b.h, a.l, b.l};
+        return make_float4(a.h, b.h, a.l, b.l);
+    }
+    __device__ __forceinline__ static store_t from_comp(const comp_t v) {
+        return make_double2(df_combine(v.x, v.z), df_combine(v.y, v.w));
     }
     __device__ __forceinline__ static void zero(acc_t& a) { a.rh = a.rl = a.ih = a.il = 0.f; }
-    __device__ __forceinline__ static void mac(acc_t& a, const mat_t m, const xval& x) {
-        df_mac(a.rh, a.rl, m.x, m.z, x.hr, x.lr);
-        df_mac(a.rh, a.rl, -m.y, -m.w, x.hi, x.li);
-        df_mac(a.ih, a.il, m.x, m.z, x.hi, x.li);
-        df_mac(a.ih, a.il, m.y, m.w, x.hr, x.lr);
+    __device__ __forceinline__ static void mac(acc_t& a, const mat_t m, const comp_t x) {
+        df_mac(a.rh, a.rl, m.x, m.z, x.x, x.z);
+        df_mac(a.rh, a.rl, -m.y, -m.w, x.y, x.w);
+        df_mac(a.ih, a.il, m.x, m.z, x.y, x.w);
+        df_mac(a.ih, a.il, m.y, m.w, x.x, x.z);
     }
-    __device__ __forceinline__ static store_t finish(acc_t& a) {
+    __device__ __forceinline__ static comp_t finish(acc_t& a) {
         df_norm(a.rh, a.rl);
         df_norm(a.ih, a.il);
-        return make_double2(df_combine(a.rh, a.rl), df_combine(a.ih, a.il));
+        return make_float4(a.rh, a.ih, a.rl, a.il);
     }
-    __device__ __forceinline__ static store_t mul(const mat_t m, const store_t v) {
+    __device__ __forceinline__ static comp_t mul(const mat_t m, const comp_t v) {
         acc_t a;
         zero(a);
-        mac(a, m, load(v));
+        mac(a, m, v);
         return finish(a);
     }
 };
 
 struct ArithF32 {
     using store_t = float2;
+    using comp_t = float2;
     using mat_t = float2;
-    struct xval { float re, im; };
     struct acc_t { float re, im; };
     static constexpr int kId = 3;
-    __device__ __forceinline__ static xval load(const store_t v) { return {v.x, v.y}; }
+    __device__ __forceinline__ static comp_t to_comp(const store_t v) { return v; }
+    __device__ __forceinline__ static store_t from_comp(const comp_t v) { return v; }
     __device__ __forceinline__ static void zero(acc_t& a) { a.re = 0.f; a.im = 0.f; }
-    __device__ __forceinline__ static void mac(acc_t& a, const mat_t m, const xval& x) {
-        a.re = fmaf(m.x, x.re, a.re);
-        a.re = fmaf(-m.y, x.im, a.re);
-        a.im = fmaf(m.x, x.im, a.im);
-        a.im = fmaf(m.y, x.re, a.im);
+    __device__ __forceinline__ static void mac(acc_t& a, const mat_t m, const comp_t x) {
+        a.re = fmaf(m.x, x.x, a.re);
+        a.re = fmaf(-m.y, x.y, a.re);
+        a.im = fmaf(m.x, x.y, a.im);
+        a.im = fmaf(m.y, x.x, a.im);
     }
-    __device__ __forceinline__ static store_t finish(acc_t& a) { return make_float2(a.re, a.im); }
-    __device__ __forceinline__ static store_t mul(const mat_t m, const store_t v) {
+    __device__ __forceinline__ static comp_t finish(acc_t& a) { return make_float2(a.re, a.im); }
+    __device__ __forceinline__ static comp_t mul(const mat_t m, const comp_t v) {
         return make_float2(fmaf(m.x, v.x, -m.y * v.y), fmaf(m.x, v.y, m.y * v.x));
     }
 };

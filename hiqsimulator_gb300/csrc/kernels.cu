@@ -94,8 +94,8 @@ cudaError_t finish_reduce(int nparts, ReduceScratch& rs, cudaStream_t s, double*
 // ---------------------------------------------------------------- fused pass
 
 template <class A>
-__device__ __forceinline__ void apply_diag(typename A::store_t* buf, const typename A::mat_t* diag,
-                                           const OpDesc& op, int Q) {
+__device__ __forceinline__ void apply_diag(typename A::comp_t* buf, const typename A::mat_t* diag, const OpDesc& op,
+                                           int Q) {
     for (int L = threadIdx.x; L < Q; L += blockDim.x) {
         if ((L & op.ctrl_local) != op.ctrl_local) continue;
         int r = 0;
@@ -105,24 +105,24 @@ __device__ __forceinline__ void apply_diag(typename A::store_t* buf, const typen
 }
 
 template <class A>
-__device__ __forceinline__ void apply_scalar(typename A::store_t* buf, const typename A::mat_t m, int Q) {
+__device__ __forceinline__ void apply_scalar(typename A::comp_t* buf, const typename A::mat_t m, int Q) {
     for (int L = threadIdx.x; L < Q; L += blockDim.x) buf[L] = A::mul(m, buf[L]);
 }
 
-// Dense k-qubit op, tile src -> tile dst. A task is (index group, block of
-// RPT output rows); consecutive threads take consecutive groups of the same
-// row block so matrix reads are shared-memory broadcasts.
-template <class A, int K>
-__device__ __forceinline__ void apply_dense(const typename A::store_t* __restrict__ src,
-                                            typename A::store_t* __restrict__ dst,
-                                            const typename A::mat_t* __restrict__ mat, const OpDesc& op, int q) {
-    using S = typename A::store_t;
+// Dense k-qubit op, tile src -> tile dst. The matrix is stored transposed
+// (matT[c * D + r] = M[r][c]). A task is one output row r for up to GPT index
+// groups; consecutive threads take consecutive rows of the same groups, so
+// every input read is a shared-memory broadcast and the matrix reads of a
+// warp are consecutive.
+template <class A, int K, int GPT>
+__device__ __forceinline__ void apply_dense(const typename A::comp_t* __restrict__ src,
+                                            typename A::comp_t* __restrict__ dst,
+                                            const typename A::mat_t* __restrict__ matT, const OpDesc& op, int q) {
+    using C = typename A::comp_t;
     constexpr int D = 1 << K;
-    constexpr int RPT = (K >= 3) ? 4 : D;
-    constexpr int LOG_RPT = (K >= 3) ? 2 : K;
-    constexpr int RB = D / RPT;
-    const int gbits = q - K;
-    const int G = 1 << gbits;
+    const int G = 1 << (q - K);
+    const int gpt = G < GPT ? G : GPT;
+    const int ntask = D * (G / gpt);
     int ss[K];
     uint32_t bitv[K];
 #pragma unroll
@@ -136,68 +136,62 @@ __device__ __forceinline__ void apply_dense(const typename A::store_t* __restric
         for (int b = K - 1; b >= a; --b)
             if (ss[b - 1] > ss[b]) { const int t = ss[b]; ss[b] = ss[b - 1]; ss[b - 1] = t; }
 
-    for (int task = threadIdx.x; task < G * RB; task += blockDim.x) {
-        const int g = task & (G - 1);
-        const int rb = task >> gbits;
-        uint32_t Lb = (uint32_t)g;
+    for (int task = threadIdx.x; task < ntask; task += blockDim.x) {
+        const int r = task & (D - 1);
+        const int g0 = (task >> K) * gpt;
+        uint32_t orow = 0;
 #pragma unroll
-        for (int j = 0; j < K; ++j) {
-            const uint32_t low = Lb & ((1u << ss[j]) - 1u);
-            Lb = ((Lb - low) << 1) | low;
-        }
-        uint32_t rowoff = 0;  // offset of row rb*RPT
+        for (int j = 0; j < K; ++j)
+            if ((r >> j) & 1) orow |= bitv[j];
+        uint32_t Lb[GPT];
+        bool ok[GPT];
 #pragma unroll
-        for (int j = LOG_RPT; j < K; ++j)
-            if (((rb * RPT) >> j) & 1) rowoff |= bitv[j];
-        if ((Lb & op.ctrl_local) != op.ctrl_local) {
+        for (int i = 0; i < GPT; ++i) {
+            uint32_t v = (uint32_t)(g0 + (i < gpt ? i : 0));
 #pragma unroll
-            for (int rr = 0; rr < RPT; ++rr) {
-                uint32_t o = rowoff;
-#pragma unroll
-                for (int j = 0; j < LOG_RPT; ++j)
-                    if ((rr >> j) & 1) o |= bitv[j];
-                dst[Lb + o] = src[Lb + o];
+            for (int j = 0; j < K; ++j) {
+                const uint32_t low = v & ((1u << ss[j]) - 1u);
+                v = ((v - low) << 1) | low;
             }
-            continue;
+            Lb[i] = v;
+            ok[i] = (i < gpt) && ((v & op.ctrl_local) == op.ctrl_local);
         }
-        typename A::xval x[D];
+        typename A::acc_t acc[GPT];
+#pragma unroll
+        for (int i = 0; i < GPT; ++i) A::zero(acc[i]);
 #pragma unroll
         for (int c = 0; c < D; ++c) {
-            uint32_t o = 0;
+            uint32_t oc = 0;
 #pragma unroll
             for (int j = 0; j < K; ++j)
-                if ((c >> j) & 1) o |= bitv[j];
-            x[c] = A::load(src[Lb + o]);
+                if ((c >> j) & 1) oc |= bitv[j];
+            const typename A::mat_t m = matT[c * D + r];
+#pragma unroll
+            for (int i = 0; i < GPT; ++i)
+                if (ok[i]) A::mac(acc[i], m, src[Lb[i] + oc]);
         }
 #pragma unroll
-        for (int rr = 0; rr < RPT; ++rr) {
-            const int r = rb * RPT + rr;
-            const typename A::mat_t* mrow = mat + r * D;
-            typename A::acc_t acc;
-            A::zero(acc);
-#pragma unroll
-            for (int c = 0; c < D; ++c) A::mac(acc, mrow[c], x[c]);
-            uint32_t o = rowoff;
-#pragma unroll
-            for (int j = 0; j < LOG_RPT; ++j)
-                if ((rr >> j) & 1) o |= bitv[j];
-            dst[Lb + o] = A::finish(acc);
+        for (int i = 0; i < GPT; ++i) {
+            if (i >= gpt) continue;
+            dst[Lb[i] + orow] = ok[i] ? A::finish(acc[i]) : src[Lb[i] + orow];
         }
     }
 }
 
+constexpr int kPassGPT = 4;
+
 template <class A>
-__global__ void __launch_bounds__(kThreads) pass_kernel(typename A::store_t* __restrict__ state,
-                                                        const typename A::mat_t* __restrict__ mats,
-                                                        const __grid_constant__ PassDesc d) {
-    using S = typename A::store_t;
+__global__ void __launch_bounds__(kThreads, 4) pass_kernel(typename A::store_t* __restrict__ state,
+                                                           const typename A::mat_t* __restrict__ mats,
+                                                           const __grid_constant__ PassDesc d) {
+    using C = typename A::comp_t;
     using M = typename A::mat_t;
     extern __shared__ __align__(16) unsigned char smem[];
     M* smat = reinterpret_cast<M*>(smem);
     const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(M) + 15) & ~(size_t)15;
     const int Q = 1 << d.q;
-    S* bufA = reinterpret_cast<S*>(smem + mat_bytes);
-    S* bufB = bufA + Q;
+    C* bufA = reinterpret_cast<C*>(smem + mat_bytes);
+    C* bufB = bufA + Q;
     uint64_t* hoff = reinterpret_cast<uint64_t*>(bufB + Q);
     const int nh = d.q - d.w;
     const uint32_t lowmask = (1u << d.w) - 1u;
@@ -217,10 +211,10 @@ __global__ void __launch_bounds__(kThreads) pass_kernel(typename A::store_t* __r
         for (int i = 0; i < d.nins; ++i) base = insert_zero(base, d.ins_pos[i]);
         base |= d.fixed_mask;
         for (int L = threadIdx.x; L < Q; L += blockDim.x)
-            bufA[L] = state[base + hoff[L >> d.w] + (L & lowmask)];
+            bufA[L] = A::to_comp(state[base + hoff[L >> d.w] + (L & lowmask)]);
         __syncthreads();
-        S* src = bufA;
-        S* dst = bufB;
+        C* src = bufA;
+        C* dst = bufB;
         for (int oi = 0; oi < d.nops; ++oi) {
             const OpDesc& op = d.ops[oi];
             if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
@@ -235,19 +229,19 @@ __global__ void __launch_bounds__(kThreads) pass_kernel(typename A::store_t* __r
                 continue;
             }
             switch (op.k) {
-                case 1: apply_dense<A, 1>(src, dst, smat + op.mat_off, op, d.q); break;
-                case 2: apply_dense<A, 2>(src, dst, smat + op.mat_off, op, d.q); break;
-                case 3: apply_dense<A, 3>(src, dst, smat + op.mat_off, op, d.q); break;
-                case 4: apply_dense<A, 4>(src, dst, smat + op.mat_off, op, d.q); break;
-                default: apply_dense<A, 5>(src, dst, smat + op.mat_off, op, d.q); break;
+                case 1: apply_dense<A, 1, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
+                case 2: apply_dense<A, 2, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
+                case 3: apply_dense<A, 3, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
+                case 4: apply_dense<A, 4, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
+                default: apply_dense<A, 5, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
             }
             __syncthreads();
-            S* tmp = src;
+            C* tmp = src;
             src = dst;
             dst = tmp;
         }
         for (int L = threadIdx.x; L < Q; L += blockDim.x)
-            state[base + hoff[L >> d.w] + (L & lowmask)] = src[L];
+            state[base + hoff[L >> d.w] + (L & lowmask)] = A::from_comp(src[L]);
         __syncthreads();
     }
 }
@@ -255,7 +249,7 @@ __global__ void __launch_bounds__(kThreads) pass_kernel(typename A::store_t* __r
 template <class A>
 size_t pass_smem_t(const PassDesc& d) {
     const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(typename A::mat_t) + 15) & ~(size_t)15;
-    return mat_bytes + 2 * (sizeof(typename A::store_t) << d.q) + sizeof(uint64_t) * (1u << (d.q - d.w));
+    return mat_bytes + 2 * (sizeof(typename A::comp_t) << d.q) + sizeof(uint64_t) * (1u << (d.q - d.w));
 }
 
 template <class A>
@@ -448,9 +442,9 @@ __global__ void __launch_bounds__(kThreads) pauli_apply_kernel(const typename A:
         for (int t = 0; t < nterms; ++t) {
             const uint64_t j = i ^ xm[t];
             const int neg = __popcll(j & (ym[t] | zm[t])) & 1;
-            A::mac(acc, coef[2 * t + neg], A::load(in[j]));
+            A::mac(acc, coef[2 * t + neg], A::to_comp(in[j]));
         }
-        out[i] = A::finish(acc);
+        out[i] = A::from_comp(A::finish(acc));
     }
 }
 
@@ -467,7 +461,7 @@ __global__ void __launch_bounds__(kThreads) collapse_kernel(typename A::store_t*
             z.y = 0;
             state[i] = z;
         } else {
-            state[i] = A::mul(scale, state[i]);
+            state[i] = A::from_comp(A::mul(scale, A::to_comp(state[i])));
         }
     }
 }

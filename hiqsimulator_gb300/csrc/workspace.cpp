@@ -118,7 +118,9 @@ std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& o
         PassPlan pl;
         PassDesc& d = pl.desc;
         std::memset(&d, 0, sizeof(d));
-        const int q = std::min(n, std::max(popc64(tset), max_tile_bits));
+        // tile: the pass's targets plus at least 4 low positions, 2^10 amplitudes
+        // at least (enough index groups for every thread), at most 2^max_tile_bits
+        const int q = std::min(n, std::max(popc64(tset), std::min(max_tile_bits, std::max(popc64(tset) + 4, 10))));
         uint64_t tile = tset;
         for (int b = 0; b < n && popc64(tile) < q; ++b) tile |= 1ULL << b;
         int slot[64];
@@ -166,7 +168,19 @@ std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& o
     return plans;
 }
 
-static void convert_matrix(int arith, const std::vector<cplx>& m, unsigned char* dst) {
+// Dense gates are stored transposed (element c * dim + r holds M[r][c]): the
+// pass kernel's threads own output rows and read one column entry per input.
+static void convert_matrix(int arith, const GateOp& op, unsigned char* dst) {
+    std::vector<cplx> t;
+    const std::vector<cplx>* src = &op.m;
+    if (op.k > 0 && !op.diag) {
+        const size_t dim = (size_t)1 << op.k;
+        t.resize(op.m.size());
+        for (size_t r = 0; r < dim; ++r)
+            for (size_t c = 0; c < dim; ++c) t[c * dim + r] = op.m[r * dim + c];
+        src = &t;
+    }
+    const std::vector<cplx>& m = *src;
     if (arith == kArithF64) {
         double* p = reinterpret_cast<double*>(dst);
         for (size_t e = 0; e < m.size(); ++e) {
@@ -211,7 +225,7 @@ uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<G
         size_t off = p.pool_off;
         for (int o = 0; o < p.desc.nops; ++o) {
             const GateOp& op = ops[first[pi] + o];
-            convert_matrix(arith, op.m, host + off);
+            convert_matrix(arith, op, host + off);
             off += op.m.size() * mat_elem_bytes(arith);
         }
     }
