@@ -34,7 +34,7 @@ Engine::Engine(uint64_t seed, int64_t max_local, int64_t max_cluster_size, int p
       rnd_eng_(seed) {
     if (arith_ == 0) arith_ = (precision_ == kC64) ? kArithF32 : kArithDF;
     if (precision_ == kC64 && arith_ != kArithF32) fail("complex64 states use FP32 arithmetic");
-    if (precision_ == kC128 && arith_ == kArithF32) fail("complex128 states use F64 or DF arithmetic");
+    if (precision_ == kC128 && arith_ == kArithF32) fail("complex128 states use F64, DF or TC arithmetic");
     capacity_ = 1024;
     cuda_check(cudaMalloc(&state_, capacity_ * elem_bytes()), "cudaMalloc(state)");
     cuda_check(cudaMemsetAsync(state_, 0, capacity_ * elem_bytes(), ws_.stream()), "cudaMemsetAsync");
@@ -540,7 +540,7 @@ void Engine::apply_qubit_operator(const std::vector<PauliTerm>& terms, const std
                 double* p = reinterpret_cast<double*>(dst);
                 p[0] = v.real();
                 p[1] = v.imag();
-            } else if (arith_ == kArithDF) {
+            } else if (arith_ == kArithDF || arith_ == kArithTC) {
                 float* p = reinterpret_cast<float*>(dst);
                 p[0] = (float)v.real();
                 p[1] = (float)v.imag();

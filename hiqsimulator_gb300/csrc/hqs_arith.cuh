@@ -171,6 +171,27 @@ struct ArithF32 {
     }
 };
 
+// complex128 tiles kept as raw doubles; each operation splits its inputs into
+// double-float pairs on the fly and re-assembles its outputs. Used by passes
+// that also run tensor-core gates, which read the raw doubles.
+struct ArithDFRaw {
+    using store_t = double2;
+    using comp_t = double2;
+    using mat_t = float4;
+    using acc_t = ArithDF::acc_t;
+    static constexpr int kId = 4;
+    __device__ __forceinline__ static comp_t to_comp(const store_t v) { return v; }
+    __device__ __forceinline__ static store_t from_comp(const comp_t v) { return v; }
+    __device__ __forceinline__ static void zero(acc_t& a) { ArithDF::zero(a); }
+    __device__ __forceinline__ static void mac(acc_t& a, const mat_t m, const comp_t x) {
+        ArithDF::mac(a, m, ArithDF::to_comp(x));
+    }
+    __device__ __forceinline__ static comp_t finish(acc_t& a) { return ArithDF::from_comp(ArithDF::finish(a)); }
+    __device__ __forceinline__ static comp_t mul(const mat_t m, const comp_t v) {
+        return ArithDF::from_comp(ArithDF::mul(m, ArithDF::to_comp(v)));
+    }
+};
+
 // -------------------------------------------------- |a|^2 accumulation policies
 // Probability-type sums are accumulated per thread to about 48 significant bits
 // (double-float for complex128 / complex64 storage in DF / F32 mode, FP64 in

@@ -21,7 +21,13 @@ enum Arith : int32_t {
     kArithF64 = 1,  // complex128 storage, native FP64 arithmetic
     kArithDF = 2,   // complex128 storage, double-float (2 x FP32) arithmetic, ~48-bit
     kArithF32 = 3,  // complex64 storage, FP32 arithmetic
+    kArithTC = 4,   // complex128 storage, dense 3..5-qubit gates on the fp16 tensor cores
+                    // (exact digit products, see apply_tc), the rest in double-float
 };
+
+// Tensor-core digit planes: every real operand is written as kTcDigits signed
+// base-2^10 digits (|d| <= 512) scaled by a power of two shared by its row.
+constexpr int kTcDigits = 5;
 
 struct OpDesc {
     int32_t k;            // targets (0 = scalar multiply of the whole tile)
@@ -30,7 +36,8 @@ struct OpDesc {
     uint32_t mat_off;     // offset (elements) of this op's matrix in the pass pool
     uint64_t ctrl_outer;  // state bits outside the tile that must all be 1
     uint8_t tslot[kMaxK]; // tile-local bit of matrix bit j
-    uint8_t pad[3];
+    uint8_t tc;           // 1: dense gate applied on the tensor cores (digit planes in the pool)
+    uint8_t pad[2];
 };
 
 struct PassDesc {
@@ -40,6 +47,8 @@ struct PassDesc {
     int32_t nops;
     int32_t nins;         // number of sorted positions in ins_pos
     uint32_t mat_elems;   // pool elements staged into shared memory
+    uint32_t tc_bytes;    // shared-memory scratch for tensor-core digit planes (0: none)
+    uint32_t pad0;
     uint64_t fixed_mask;  // state bits forced to 1 for every processed tile
     uint8_t tile_pos[kMaxTileBits];
     uint8_t ins_pos[64];  // sorted union of tile_pos and fixed-mask positions

@@ -5,6 +5,7 @@
 // src/simulator-mpi/SimulatorMPI.cpp (getProbability_internal :841-870,
 // normalize :872-895, calcLocalApproxDistribution :817-839, Entropy :681-694,
 // DeallocateLocalQubit :278-322) with tiled, coalesced passes over HBM.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -178,10 +179,221 @@ __device__ __forceinline__ void apply_dense(const typename A::comp_t* __restrict
     }
 }
 
+
+// ------------------------------------------------------------ tensor-core gates
+//
+// A dense k-qubit gate (k = 3..5) on a tile of G = 2^(q-k) index groups is the
+// real GEMM  Y[G x 2D] = X[G x 2D] * B[2D x 2D],  D = 2^k, with X holding the
+// real then imaginary parts of each group's inputs and B the real form of the
+// gate ([Re M^T, Im M^T; -Im M^T, Re M^T]). Every entry of X is written as
+// 2^E_row * sum_i d_i 2^(-9-10i) with five signed digits |d_i| <= 512 (E_row
+// shared by the row), every entry of B likewise with E_col shared by the
+// column (digits computed on the host). Digits are exact in fp16, a product
+// of two digits has at most 18 bits and a 2D <= 64 term sum at most 24 bits,
+// so the fp32 accumulation of one digit pair is exact. Pairs (i, j) with
+// i + j <= 2 get their own accumulators, the pairs of levels 3 and 4 share one
+// each (their rounding is below 2^-46 of the row scale), levels >= 5 are
+// dropped (below 2^-47 of it). The epilogue adds the eight accumulators in
+// double-float and re-assembles doubles with integer operations.
+
+__device__ __forceinline__ uint32_t pack_digits(int d0, int d1) {
+    const float f0 = __int_as_float(0x4B400000 + d0) - 12582912.0f;
+    const float f1 = __int_as_float(0x4B400000 + d1) - 12582912.0f;
+    __half2 h = __floats2half2_rn(f0, f1);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// Digits of v relative to the row's largest biased exponent ebrow
+// (|v| < 2^(ebrow - 1022)), most significant first.
+__device__ __forceinline__ void digits5(double v, int ebrow, int (&d)[kTcDigits]) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
+    const int eb = (int)((u >> 52) & 0x7FFu);
+    long long X = 0;
+    if (eb != 0) {
+        const long long M = (long long)((u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52));
+        const int sh = 4 + ebrow - eb;  // X = round(v * 2^(49 - E_row)) = round(M / 2^sh)
+        if (sh < 62) X = (M + (1LL << (sh - 1))) >> sh;
+        if (u >> 63) X = -X;
+    }
+#pragma unroll
+    for (int i = kTcDigits - 1; i >= 1; --i) {
+        const int dd = (int)((X + 512) & 1023) - 512;
+        d[i] = dd;
+        X = (X - dd) >> 10;
+    }
+    d[0] = (int)X;
+}
+
+__device__ __forceinline__ float scale_pow2(float x, int s) {
+    if (s > 120) { x *= 0x1p120f; s -= 120; }
+    if (s < -120) { x *= 0x1p-120f; s += 120; }
+    if (s < -126) return 0.f;
+    return x * __int_as_float((s + 127) << 23);
+}
+
+__device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
+}
+
+__device__ __forceinline__ void mma_f16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+                 "{%0,%1,%2,%3};"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// accumulator of digit pair (i, j) and its level i + j
+__host__ __device__ constexpr int tc_acc(int i, int j) {
+    return (i + j == 0) ? 0 : (i + j == 1) ? 1 + i : (i + j == 2) ? 3 + i : (i + j == 3) ? 6 : 7;
+}
+__host__ __device__ constexpr int tc_level(int a) { return a == 0 ? 0 : a <= 2 ? 1 : a <= 5 ? 2 : a == 6 ? 3 : 4; }
+
+// Pool layout of a tensor-core gate (bytes): int32 E_col[2D], then kTcDigits
+// planes of B^T, each 2D rows of (2D + 8) fp16 (row j holds column j of B).
+template <int K>
+__device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double2* __restrict__ dst,
+                                         const unsigned char* __restrict__ pool, const OpDesc& op, int q,
+                                         unsigned char* __restrict__ scratch) {
+    constexpr int D = 1 << K;
+    constexpr int KK = 2 * D;
+    constexpr int RH = KK + 8;  // fp16 per plane row (padded against bank conflicts)
+    const int G = 1 << (q - K);
+    const int* ecol = reinterpret_cast<const int*>(pool);
+    const __half* planeB = reinterpret_cast<const __half*>(pool + 4 * KK);
+    __half* planeA = reinterpret_cast<__half*>(scratch);
+    int* erow = reinterpret_cast<int*>(scratch + (size_t)kTcDigits * G * RH * 2);
+    const double* srcd = reinterpret_cast<const double*>(src);
+    double* dstd = reinterpret_cast<double*>(dst);
+
+    int ss[K];
+    uint32_t bitv[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        ss[j] = op.tslot[j];
+        bitv[j] = 1u << op.tslot[j];
+    }
+#pragma unroll
+    for (int a = 1; a < K; ++a)
+#pragma unroll
+        for (int b = K - 1; b >= a; --b)
+            if (ss[b - 1] > ss[b]) { const int t = ss[b]; ss[b] = ss[b - 1]; ss[b - 1] = t; }
+    auto group_base = [&](uint32_t g) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const uint32_t low = g & ((1u << ss[j]) - 1u);
+            g = ((g - low) << 1) | low;
+        }
+        return g;
+    };
+    auto offset_of = [&](int c) {
+        uint32_t o = 0;
+#pragma unroll
+        for (int j = 0; j < K; ++j)
+            if ((c >> j) & 1) o |= bitv[j];
+        return o;
+    };
+
+    // 1. row exponents: the largest biased exponent of each group's 2D reals
+    for (int g = threadIdx.x; g < G; g += blockDim.x) erow[g] = 0;
+    __syncthreads();
+    for (int v = threadIdx.x; v < G * KK; v += blockDim.x) {
+        const int g = v / KK, kk = v % KK;
+        const double x = srcd[2 * (group_base(g) + offset_of(kk & (D - 1))) + (kk >> K)];
+        const int eb = (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FFu);
+        if (eb) atomicMax(&erow[g], eb);
+    }
+    __syncthreads();
+    // 2. digit planes of X (two reals per thread step, packed as half2)
+    for (int v = threadIdx.x; v < G * (KK / 2); v += blockDim.x) {
+        const int g = v / (KK / 2), kk = 2 * (v % (KK / 2));
+        const uint32_t Lb = group_base(g);
+        const double x0 = srcd[2 * (Lb + offset_of(kk & (D - 1))) + (kk >> K)];
+        const double x1 = srcd[2 * (Lb + offset_of((kk + 1) & (D - 1))) + ((kk + 1) >> K)];
+        int d0[kTcDigits], d1[kTcDigits];
+        digits5(x0, erow[g], d0);
+        digits5(x1, erow[g], d1);
+#pragma unroll
+        for (int s = 0; s < kTcDigits; ++s)
+            *reinterpret_cast<uint32_t*>(planeA + (size_t)s * G * RH + (size_t)g * RH + kk) = pack_digits(d0[s], d1[s]);
+    }
+    __syncthreads();
+
+    // 3. MMA: warp task = (16 groups) x (16 output reals)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int mtiles = G / 16;
+    constexpr int NP = KK / 16;
+    for (int task = warp; task < mtiles * NP; task += nwarps) {
+        const int mt = task / NP, np = task % NP;
+        float acc[8][2][4];
+#pragma unroll
+        for (int a = 0; a < 8; ++a)
+#pragma unroll
+            for (int n = 0; n < 2; ++n)
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[a][n][e] = 0.f;
+#pragma unroll
+        for (int ks = 0; ks < KK / 16; ++ks) {
+            uint32_t af[kTcDigits][4];
+            const int arow = mt * 16 + (lane & 7) + ((lane >> 3) & 1) * 8;
+            const int acol = ks * 16 + (lane >> 4) * 8;
+#pragma unroll
+            for (int s = 0; s < kTcDigits; ++s) ldsm_x4(af[s], planeA + (size_t)s * G * RH + (size_t)arow * RH + acol);
+            const int brow = (np * 2 + (lane >> 4)) * 8 + (lane & 7);
+            const int bcol = ks * 16 + ((lane >> 3) & 1) * 8;
+#pragma unroll
+            for (int j = 0; j < kTcDigits; ++j) {
+                uint32_t bf[4];
+                ldsm_x4(bf, planeB + (size_t)j * KK * RH + (size_t)brow * RH + bcol);
+#pragma unroll
+                for (int i = 0; i + j < kTcDigits; ++i) {
+                    const int a = tc_acc(i, j);
+                    mma_f16(acc[a][0], af[i], bf[0], bf[1]);
+                    mma_f16(acc[a][1], af[i], bf[2], bf[3]);
+                }
+            }
+        }
+        // 4. epilogue: rows g0, g0 + 8; columns (np*2 + n)*8 + 2*tig + {0, 1}
+        const int gid = lane >> 2, tig = lane & 3;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int g = mt * 16 + gid + h * 8;
+            const uint32_t Lb = group_base(g);
+            const bool ok = (Lb & op.ctrl_local) == op.ctrl_local;
+            const int er = erow[g] - 1022;
+#pragma unroll
+            for (int n = 0; n < 2; ++n)
+#pragma unroll
+                for (int c2 = 0; c2 < 2; ++c2) {
+                    const int jj = (np * 2 + n) * 8 + tig * 2 + c2;
+                    const int r = jj & (D - 1), part = jj >> K;
+                    const size_t di = 2 * (size_t)(Lb + offset_of(r)) + part;
+                    if (!ok) {
+                        dstd[di] = srcd[di];
+                        continue;
+                    }
+                    const int base = er + ecol[jj] - 18;
+                    float sh = 0.f, sl = 0.f;
+#pragma unroll
+                    for (int a = 0; a < 8; ++a) {
+                        const float f = scale_pow2(acc[a][n][h * 2 + c2], base - 10 * tc_level(a));
+                        const float t = sh + f;
+                        const float bb = t - sh;
+                        sl += (sh - (t - bb)) + (f - bb);
+                        sh = t;
+                    }
+                    df_norm(sh, sl);
+                    dstd[di] = df_combine(sh, sl);
+                }
+        }
+    }
+}
+
 constexpr int kPassGPT = 4;
 
 template <class A>
-__global__ void __launch_bounds__(kThreads, 4) pass_kernel(typename A::store_t* __restrict__ state,
+__global__ void __launch_bounds__(kThreads, A::kId == 4 ? 2 : 4) pass_kernel(typename A::store_t* __restrict__ state,
                                                            const typename A::mat_t* __restrict__ mats,
                                                            const __grid_constant__ PassDesc d) {
     using C = typename A::comp_t;
@@ -195,6 +407,9 @@ __global__ void __launch_bounds__(kThreads, 4) pass_kernel(typename A::store_t* 
     uint64_t* hoff = reinterpret_cast<uint64_t*>(bufB + Q);
     const int nh = d.q - d.w;
     const uint32_t lowmask = (1u << d.w) - 1u;
+    // tensor-core scratch, 16-byte aligned for ldmatrix
+    unsigned char* tcs = smem + ((mat_bytes + 2 * sizeof(C) * (size_t)Q + sizeof(uint64_t) * ((size_t)1 << nh) + 15) &
+                                 ~(size_t)15);
 
     for (uint32_t i = threadIdx.x; i < d.mat_elems; i += blockDim.x) smat[i] = mats[i];
     for (int j = threadIdx.x; j < (1 << nh); j += blockDim.x) {
@@ -228,6 +443,21 @@ __global__ void __launch_bounds__(kThreads, 4) pass_kernel(typename A::store_t* 
                 __syncthreads();
                 continue;
             }
+            if constexpr (A::kId == 4) {
+                if (op.tc) {
+                    const unsigned char* pool = reinterpret_cast<const unsigned char*>(smat + op.mat_off);
+                    switch (op.k) {
+                        case 3: apply_tc<3>(src, dst, pool, op, d.q, tcs); break;
+                        case 4: apply_tc<4>(src, dst, pool, op, d.q, tcs); break;
+                        default: apply_tc<5>(src, dst, pool, op, d.q, tcs); break;
+                    }
+                    __syncthreads();
+                    C* tmp = src;
+                    src = dst;
+                    dst = tmp;
+                    continue;
+                }
+            }
             switch (op.k) {
                 case 1: apply_dense<A, 1, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
                 case 2: apply_dense<A, 2, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
@@ -249,7 +479,8 @@ __global__ void __launch_bounds__(kThreads, 4) pass_kernel(typename A::store_t* 
 template <class A>
 size_t pass_smem_t(const PassDesc& d) {
     const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(typename A::mat_t) + 15) & ~(size_t)15;
-    return mat_bytes + 2 * (sizeof(typename A::comp_t) << d.q) + sizeof(uint64_t) * (1u << (d.q - d.w));
+    return ((mat_bytes + 2 * (sizeof(typename A::comp_t) << d.q) + sizeof(uint64_t) * (1u << (d.q - d.w)) + 15) &
+            ~(size_t)15) + d.tc_bytes;
 }
 
 template <class A>
@@ -561,10 +792,14 @@ int device_sm_count() {
     return sms;
 }
 
+// Kernels other than the fused pass treat tensor-core mode as double-float.
+static inline int base_arith(int a) { return a == kArithTC ? kArithDF : a; }
+
 size_t pass_smem_bytes(int arith, const PassDesc& d) {
     switch (arith) {
         case kArithF64: return pass_smem_t<ArithF64>(d);
         case kArithDF: return pass_smem_t<ArithDF>(d);
+        case kArithTC: return pass_smem_t<ArithDFRaw>(d);
         default: return pass_smem_t<ArithF32>(d);
     }
 }
@@ -574,12 +809,14 @@ cudaError_t launch_pass(int arith, void* state, const void* mats, const PassDesc
         case kArithF64: return launch_pass_t<ArithF64>(state, mats, d, s);
         case kArithDF: return launch_pass_t<ArithDF>(state, mats, d, s);
         case kArithF32: return launch_pass_t<ArithF32>(state, mats, d, s);
+        case kArithTC: return launch_pass_t<ArithDFRaw>(state, mats, d, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
 cudaError_t reduce_probability(int arith, const void* state, int n, uint64_t mask, uint64_t val,
                                ReduceScratch& rs, cudaStream_t s, double* out) {
+    arith = base_arith(arith);
     const MaskSpec m = make_mask_spec(mask, val);
     const uint64_t count = (1ULL << n) >> m.npos;
     const int g = reduce_grid(count);
@@ -596,6 +833,7 @@ cudaError_t reduce_probability(int arith, const void* state, int n, uint64_t mas
 
 cudaError_t reduce_bit_probs(int arith, const void* state, int n, int pos, ReduceScratch& rs, cudaStream_t s,
                              double* out2) {
+    arith = base_arith(arith);
     const uint64_t count = 1ULL << n;
     const int g = reduce_grid(count);
     if (arith == kArithF64)
@@ -610,6 +848,7 @@ cudaError_t reduce_bit_probs(int arith, const void* state, int n, int pos, Reduc
 }
 
 cudaError_t reduce_entropy(int arith, const void* state, int n, ReduceScratch& rs, cudaStream_t s, double* out) {
+    arith = base_arith(arith);
     const uint64_t count = 1ULL << n;
     const int g = reduce_grid(count);
     if (arith == kArithF64)
@@ -626,6 +865,7 @@ cudaError_t reduce_entropy(int arith, const void* state, int n, ReduceScratch& r
 }
 
 cudaError_t block_sums(int arith, const void* state, int n, uint64_t nblocks, double* d_out, cudaStream_t s) {
+    arith = base_arith(arith);
     const uint64_t K = (1ULL << n) / nblocks;
     if (K >= kThreads) {
         if (arith == kArithF64)
@@ -649,6 +889,7 @@ cudaError_t block_sums(int arith, const void* state, int n, uint64_t nblocks, do
 cudaError_t reduce_pauli_expectation(int arith, const void* state, int n, int nterms, const uint64_t* d_xm,
                                      const uint64_t* d_ym, const uint64_t* d_zm, const double* d_coef,
                                      ReduceScratch& rs, cudaStream_t s, double* out) {
+    arith = base_arith(arith);
     const uint64_t count = 1ULL << n;
     const int g = reduce_grid(count);
     if (arith == kArithF32)
@@ -664,6 +905,7 @@ cudaError_t reduce_pauli_expectation(int arith, const void* state, int n, int nt
 
 cudaError_t pauli_apply(int arith, const void* in, void* out, int n, int nterms, const uint64_t* d_xm,
                         const uint64_t* d_ym, const uint64_t* d_zm, const double* d_coef, cudaStream_t s) {
+    arith = base_arith(arith);
     const uint64_t count = 1ULL << n;
     const int g = stream_grid(count);
     if (arith == kArithF64)
@@ -680,6 +922,7 @@ cudaError_t pauli_apply(int arith, const void* in, void* out, int n, int nterms,
 
 cudaError_t collapse_scale(int arith, void* state, int n, uint64_t mask, uint64_t val, double scale,
                            cudaStream_t s) {
+    arith = base_arith(arith);
     const uint64_t count = 1ULL << n;
     const int g = stream_grid(count);
     if (arith == kArithF64) {
@@ -696,6 +939,7 @@ cudaError_t collapse_scale(int arith, void* state, int n, uint64_t mask, uint64_
 }
 
 cudaError_t fill_value(int arith, void* state, uint64_t count, double re, double im, cudaStream_t s) {
+    arith = base_arith(arith);
     const int g = stream_grid(count);
     if (arith == kArithF32)
         fill_kernel<float2><<<g, kThreads, 0, s>>>((float2*)state, count, make_float2((float)re, (float)im));
@@ -705,6 +949,7 @@ cudaError_t fill_value(int arith, void* state, uint64_t count, double re, double
 }
 
 cudaError_t drop_bit(int arith, void* state, int n, int pos, int keep, cudaStream_t s) {
+    arith = base_arith(arith);
     // windows [lo, hi) whose sources lie entirely above hi (see kernel comment)
     const uint64_t keepbit = keep ? (1ULL << pos) : 0ULL;
     const uint64_t half = 1ULL << (n - 1);
@@ -722,6 +967,7 @@ cudaError_t drop_bit(int arith, void* state, int n, int pos, int keep, cudaStrea
 
 cudaError_t permute_bits(int arith, void* state, int n, int m, const uint8_t* oldpos, const uint8_t* newpos,
                          cudaStream_t s) {
+    arith = base_arith(arith);
     if (m == 0) return cudaSuccess;
     PermSpec p;
     p.n = n;

@@ -109,7 +109,7 @@ extern "C" int hqs_probability_noalloc(const void* state, int n, int arith, uint
                                        double* d_out, void* stream) {
     if (!state || !d_out) return fail(HQS_ERR_INVALID, "hqs_probability_noalloc: null state or output pointer");
     if (n < 0 || n > 40) return fail(HQS_ERR_INVALID, "hqs_probability_noalloc: n out of range");
-    if (arith != HQS_ARITH_F64 && arith != HQS_ARITH_DF && arith != HQS_ARITH_F32)
+    if (arith != HQS_ARITH_F64 && arith != HQS_ARITH_DF && arith != HQS_ARITH_F32 && arith != HQS_ARITH_TC)
         return fail(HQS_ERR_INVALID, "hqs_probability_noalloc: unknown arithmetic");
     if (n < 64 && (mask >> n) != 0) return fail(HQS_ERR_INVALID, "hqs_probability_noalloc: mask out of range");
     NoAllocMask m;
@@ -144,7 +144,7 @@ extern "C" int hqs_probability_noalloc(const void* state, int n, int arith, uint
     const unsigned grid = (unsigned)(nparts ? nparts : 1);
     if (arith == HQS_ARITH_F64)
         prob_chunk_kernel<hqs::NormAccF64, double2><<<grid, kThreads, 0, s>>>((const double2*)state, count, m, partials);
-    else if (arith == HQS_ARITH_DF)
+    else if (arith == HQS_ARITH_DF || arith == HQS_ARITH_TC)
         prob_chunk_kernel<hqs::NormAccDF, double2><<<grid, kThreads, 0, s>>>((const double2*)state, count, m, partials);
     else
         prob_chunk_kernel<hqs::NormAccDF, float2><<<grid, kThreads, 0, s>>>((const float2*)state, count, m, partials);

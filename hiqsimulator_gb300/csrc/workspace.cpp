@@ -91,6 +91,22 @@ void Workspace::ensure_pinned(size_t bytes) {
 
 static int popc64(uint64_t v) { return __builtin_popcountll(v); }
 
+// Pool bytes of a tensor-core gate: int32 E_col[2D] + kTcDigits planes of
+// 2D rows x (2D + 8) fp16.
+static size_t tc_pool_bytes(int k) {
+    const size_t KK = (size_t)2 << k;
+    return 4 * KK + (size_t)kTcDigits * KK * (KK + 8) * 2;
+}
+
+static bool tc_candidate(int arith, const GateOp& op) { return arith == kArithTC && !op.diag && op.k >= 3; }
+
+// Pool elements (of mat_elem_bytes) an op occupies.
+static size_t pool_elems(int arith, const GateOp& op, bool tc) {
+    const size_t melem = Workspace::mat_elem_bytes(arith);
+    if (tc) return (tc_pool_bytes(op.k) + melem - 1) / melem;
+    return op.m.size();
+}
+
 std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits, int max_ops,
                                   std::vector<size_t>* op_first) {
     const size_t melem = Workspace::mat_elem_bytes(arith);
@@ -109,7 +125,7 @@ std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& o
             uint64_t tm = 0;
             for (int t = 0; t < op.k; ++t) tm |= 1ULL << op.pos[t];
             const uint64_t ns = tset | tm;
-            const size_t ob = op.m.size() * melem;
+            const size_t ob = pool_elems(arith, op, tc_candidate(arith, op)) * melem;
             if (j > i && (popc64(ns) + 4 > max_tile_bits || mbytes + ob > mat_budget)) break;
             tset = ns;
             mbytes += ob;
@@ -144,11 +160,18 @@ std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& o
             if ((ins >> b) & 1ULL) d.ins_pos[d.nins++] = (uint8_t)b;
         d.nops = (int)(j - i);
         uint32_t moff = 0;
+        size_t tcb = 0;
         for (size_t o = i; o < j; ++o) {
             const GateOp& op = ops[o];
             OpDesc& od = d.ops[o - i];
             od.k = op.k;
             od.diag = op.diag ? 1 : 0;
+            // tensor-core gates need at least 16 index groups per tile
+            od.tc = (tc_candidate(arith, op) && q >= op.k + 4) ? 1 : 0;
+            if (od.tc) {
+                const size_t G = (size_t)1 << (q - op.k), KK = (size_t)2 << op.k;
+                tcb = std::max(tcb, (size_t)kTcDigits * G * (KK + 8) * 2 + 4 * G);
+            }
             od.ctrl_outer = op.ctrl_mask & ~tile;
             uint32_t cl = 0;
             for (int b = 0; b < n; ++b)
@@ -156,9 +179,10 @@ std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& o
             od.ctrl_local = cl;
             for (int t = 0; t < op.k; ++t) od.tslot[t] = (uint8_t)slot[op.pos[t]];
             od.mat_off = moff;
-            moff += (uint32_t)op.m.size();
+            moff += (uint32_t)pool_elems(arith, op, od.tc != 0);
         }
         d.mat_elems = moff;
+        d.tc_bytes = (uint32_t)((tcb + 15) & ~(size_t)15);
         pl.pool_off = pool_off;
         pool_off += ((size_t)moff * melem + 255) & ~(size_t)255;
         pl.bytes = 2ULL * (1ULL << (n - popc64(fixed))) * store;
@@ -166,6 +190,66 @@ std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& o
         i = j;
     }
     return plans;
+}
+
+static uint16_t half_of_int(int d) {
+    if (d == 0) return 0;
+    const uint16_t sgn = d < 0 ? 0x8000 : 0;
+    const int a = d < 0 ? -d : d;
+    const int e = 31 - __builtin_clz((unsigned)a);
+    return (uint16_t)(sgn | ((e + 15) << 10) | ((a << (10 - e)) & 0x3FF));
+}
+
+static int biased_exponent(double v) {
+    uint64_t u;
+    std::memcpy(&u, &v, 8);
+    return (int)((u >> 52) & 0x7FF);
+}
+
+// The five balanced base-2^10 digits of v relative to the biased exponent
+// ebmax of its column (same rule as the device-side digits of the state).
+static void digits_host(double v, int ebmax, int* d) {
+    uint64_t u;
+    std::memcpy(&u, &v, 8);
+    const int eb = (int)((u >> 52) & 0x7FF);
+    long long X = 0;
+    if (eb != 0) {
+        const long long M = (long long)((u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52));
+        const int sh = 4 + ebmax - eb;
+        if (sh < 62) X = (M + (1LL << (sh - 1))) >> sh;
+        if (u >> 63) X = -X;
+    }
+    for (int i = kTcDigits - 1; i >= 1; --i) {
+        const int dd = (int)((X + 512) & 1023) - 512;
+        d[i] = dd;
+        X = (X - dd) >> 10;
+    }
+    d[0] = (int)X;
+}
+
+// Real form of a complex gate for the tensor-core path: rows kk of B are the
+// real (kk < D) then imaginary inputs, columns j the real (j < D) then
+// imaginary outputs.
+static void convert_tc(const GateOp& op, unsigned char* dst) {
+    const int D = 1 << op.k, KK = 2 * D, RH = KK + 8;
+    auto bval = [&](int kk, int j) -> double {
+        const cplx m = op.m[(size_t)(j & (D - 1)) * D + (kk & (D - 1))];
+        if (kk < D) return j < D ? m.real() : m.imag();
+        return j < D ? -m.imag() : m.real();
+    };
+    int32_t* ecol = reinterpret_cast<int32_t*>(dst);
+    uint16_t* planes = reinterpret_cast<uint16_t*>(dst + 4 * KK);
+    std::memset(planes, 0, (size_t)kTcDigits * KK * RH * 2);
+    for (int j = 0; j < KK; ++j) {
+        int ebmax = 0;
+        for (int kk = 0; kk < KK; ++kk) ebmax = std::max(ebmax, biased_exponent(bval(kk, j)));
+        ecol[j] = ebmax - 1022;
+        for (int kk = 0; kk < KK; ++kk) {
+            int d[kTcDigits];
+            digits_host(bval(kk, j), ebmax, d);
+            for (int s2 = 0; s2 < kTcDigits; ++s2) planes[(size_t)s2 * KK * RH + (size_t)j * RH + kk] = half_of_int(d[s2]);
+        }
+    }
 }
 
 // Dense gates are stored transposed (element c * dim + r holds M[r][c]): the
@@ -187,7 +271,7 @@ static void convert_matrix(int arith, const GateOp& op, unsigned char* dst) {
             p[2 * e] = m[e].real();
             p[2 * e + 1] = m[e].imag();
         }
-    } else if (arith == kArithDF) {
+    } else if (arith == kArithDF || arith == kArithTC) {
         float* p = reinterpret_cast<float*>(dst);
         for (size_t e = 0; e < m.size(); ++e) {
             const double re = m[e].real(), im = m[e].imag();
@@ -225,8 +309,10 @@ uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<G
         size_t off = p.pool_off;
         for (int o = 0; o < p.desc.nops; ++o) {
             const GateOp& op = ops[first[pi] + o];
-            convert_matrix(arith, op, host + off);
-            off += op.m.size() * mat_elem_bytes(arith);
+            const bool tc = p.desc.ops[o].tc != 0;
+            if (tc) convert_tc(op, host + off);
+            else convert_matrix(arith, op, host + off);
+            off += pool_elems(arith, op, tc) * mat_elem_bytes(arith);
         }
     }
     cuda_check(cudaMemcpyAsync(pool_, pinned_, total, cudaMemcpyHostToDevice, stream_), "cudaMemcpyAsync(matrices)");

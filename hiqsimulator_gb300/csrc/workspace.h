@@ -58,7 +58,7 @@ public:
     // workspace (reused between calls; valid until the next upload).
     void* upload(const void* host, size_t bytes);
 
-    static size_t mat_elem_bytes(int arith) { return arith == kArithDF ? 16 : (arith == kArithF64 ? 16 : 8); }
+    static size_t mat_elem_bytes(int arith) { return arith == kArithF32 ? 8 : 16; }
 
     // Per-launch device timing of the apply passes (CUDA events around each
     // launch on the workspace stream). collect_timing() waits for the events,

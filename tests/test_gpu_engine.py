@@ -34,7 +34,7 @@ def Rz(t):
     return np.array([[cmath.exp(-0.5j * t), 0], [0, cmath.exp(0.5j * t)]])
 
 
-@pytest.fixture(params=["df", "f64"])
+@pytest.fixture(params=["tc", "df", "f64"])
 def make(request, hqs, cuda):
     def f(seed=1, max_local=24, cluster=4):
         return hqs.SimulatorMPI(seed, max_local, cluster, "c128", request.param)

@@ -67,7 +67,7 @@ def ws(hqs, cuda):
     w.close()
 
 
-@pytest.mark.parametrize("arith", ["f64", "df", "f32"])
+@pytest.mark.parametrize("arith", ["f64", "df", "tc", "f32"])
 @pytest.mark.parametrize("n", [1, 3, 6, 11, 14])
 def test_single_gates_match_oracle(ws, cuda, oracle_lib, arith, n):
     rng = np.random.Generator(np.random.PCG64(1000 + n))
@@ -84,7 +84,7 @@ def test_single_gates_match_oracle(ws, cuda, oracle_lib, arith, n):
             assert err < (C64_TOL if arith == "f32" else C128_TOL), (arith, n, k, diag, err)
 
 
-@pytest.mark.parametrize("arith", ["f64", "df", "f32"])
+@pytest.mark.parametrize("arith", ["f64", "df", "tc", "f32"])
 @pytest.mark.parametrize("n,tile", [(12, 11), (16, 11), (16, 8), (20, 12)])
 def test_fused_passes_match_sequential_oracle(ws, cuda, oracle_lib, arith, n, tile):
     """Many gates planned into multi-gate tiled passes equal the gates applied
@@ -189,3 +189,21 @@ def test_df_arith_roundtrip_exactness(ws, cuda):
     ws.apply_gates(d.ptr, n, "df", [(1, [3], 0, False, np.eye(2))])
     rel = np.abs(d.host() - psi) / np.maximum(np.abs(psi), 1e-300)
     assert np.max(rel) < 2.0 ** -45
+
+
+@pytest.mark.parametrize("k", [3, 4, 5])
+def test_tensor_core_gates_on_wide_dynamic_range(ws, cuda, oracle_lib, k):
+    """Dense gates on the tensor-core path (digit products) stay within the
+    complex128 tolerance when amplitudes inside one index group differ by many
+    orders of magnitude, and with controls inside and outside the tile."""
+    rng = np.random.Generator(np.random.PCG64(50 + k))
+    n = 16
+    for trial in range(3):
+        psi = rand_state(rng, n) * np.exp(rng.uniform(-25, 0, 1 << n))
+        psi /= np.linalg.norm(psi)
+        gate = rand_gate(rng, n, k, with_ctrl=True)
+        d = Dev(cuda, psi)
+        ws.apply_gates(d.ptr, n, "tc", [gate])
+        ref = psi.copy()
+        oracle_apply(oracle_lib, ref, gate)
+        assert np.max(np.abs(d.host() - ref)) < C128_TOL
