@@ -318,7 +318,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--arith", default="df", choices=["df", "f64"])
+    ap.add_argument("--arith", default="tc", choices=["tc", "df", "f64"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--defer", type=int, default=8, help="fused gates queued before the engine launches")
     ap.add_argument("--qubits", type=int, default=30, help="state size (30 is the benchmark configuration)")

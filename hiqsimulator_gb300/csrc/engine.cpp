@@ -32,7 +32,7 @@ Engine::Engine(uint64_t seed, int64_t max_local, int64_t max_cluster_size, int p
       max_local_(max_local),
       max_cluster_(max_cluster_size),
       rnd_eng_(seed) {
-    if (arith_ == 0) arith_ = (precision_ == kC64) ? kArithF32 : kArithDF;
+    if (arith_ == 0) arith_ = (precision_ == kC64) ? kArithF32 : kArithTC;
     if (precision_ == kC64 && arith_ != kArithF32) fail("complex64 states use FP32 arithmetic");
     if (precision_ == kC128 && arith_ == kArithF32) fail("complex128 states use F64, DF or TC arithmetic");
     capacity_ = 1024;

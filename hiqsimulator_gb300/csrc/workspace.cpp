@@ -136,7 +136,25 @@ std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& o
         std::memset(&d, 0, sizeof(d));
         // tile: the pass's targets plus at least 4 low positions, 2^10 amplitudes
         // at least (enough index groups for every thread), at most 2^max_tile_bits
-        const int q = std::min(n, std::max(popc64(tset), std::min(max_tile_bits, std::max(popc64(tset) + 4, 10))));
+        int q = std::min(n, std::max(popc64(tset), std::min(max_tile_bits, std::max(popc64(tset) + 4, 10))));
+        // keep the pass within one CTA's shared memory: shrink the tile (not
+        // below the targets), then give up tensor-core gates if still too big
+        bool allow_tc = true;
+        auto smem_estimate = [&](int qq, bool tcok) {
+            size_t mat = 0, tcb = 0;
+            for (size_t o = i; o < j; ++o) {
+                const bool tc = tcok && tc_candidate(arith, ops[o]) && qq >= ops[o].k + 4;
+                mat += pool_elems(arith, ops[o], tc) * melem;
+                if (tc) {
+                    const size_t G = (size_t)1 << (qq - ops[o].k), KK = (size_t)2 << ops[o].k;
+                    tcb = std::max(tcb, (size_t)kTcDigits * G * (KK + 8) * 2 + 4 * G);
+                }
+            }
+            return mat + 2 * (store << qq) + 8 * ((size_t)1 << qq) + 32 + tcb;
+        };
+        const size_t smem_budget = 200 * 1024;
+        while (smem_estimate(q, allow_tc) > smem_budget && q > std::max(popc64(tset), std::min(n, 10))) --q;
+        if (smem_estimate(q, allow_tc) > smem_budget) allow_tc = false;
         uint64_t tile = tset;
         for (int b = 0; b < n && popc64(tile) < q; ++b) tile |= 1ULL << b;
         int slot[64];
@@ -167,7 +185,7 @@ std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& o
             od.k = op.k;
             od.diag = op.diag ? 1 : 0;
             // tensor-core gates need at least 16 index groups per tile
-            od.tc = (tc_candidate(arith, op) && q >= op.k + 4) ? 1 : 0;
+            od.tc = (allow_tc && tc_candidate(arith, op) && q >= op.k + 4) ? 1 : 0;
             if (od.tc) {
                 const size_t G = (size_t)1 << (q - op.k), KK = (size_t)2 << op.k;
                 tcb = std::max(tcb, (size_t)kTcDigits * G * (KK + 8) * 2 + 4 * G);
