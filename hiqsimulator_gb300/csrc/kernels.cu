@@ -295,28 +295,29 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
         return o;
     };
 
-    // 1. row exponents: the largest biased exponent of each group's 2D reals
-    for (int g = threadIdx.x; g < G; g += blockDim.x) erow[g] = 0;
-    __syncthreads();
-    for (int v = threadIdx.x; v < G * KK; v += blockDim.x) {
-        const int g = v / KK, kk = v % KK;
-        const double x = srcd[2 * (group_base(g) + offset_of(kk & (D - 1))) + (kk >> K)];
-        const int eb = (int)(((unsigned long long)__double_as_longlong(x) >> 52) & 0x7FFu);
-        if (eb) atomicMax(&erow[g], eb);
-    }
-    __syncthreads();
-    // 2. digit planes of X (two reals per thread step, packed as half2)
-    for (int v = threadIdx.x; v < G * (KK / 2); v += blockDim.x) {
-        const int g = v / (KK / 2), kk = 2 * (v % (KK / 2));
-        const uint32_t Lb = group_base(g);
-        const double x0 = srcd[2 * (Lb + offset_of(kk & (D - 1))) + (kk >> K)];
-        const double x1 = srcd[2 * (Lb + offset_of((kk + 1) & (D - 1))) + ((kk + 1) >> K)];
-        int d0[kTcDigits], d1[kTcDigits];
-        digits5(x0, erow[g], d0);
-        digits5(x1, erow[g], d1);
+    // 1. digit planes of X: a group's 2D reals are handled by KK/2 consecutive
+    // lanes (two reals each); the row exponent is a max over those lanes.
+    {
+        constexpr int LPG = KK / 2;  // lanes per group (8, 16 or 32)
+        const int lane = threadIdx.x & 31;
+        for (int v = threadIdx.x; v < G * LPG; v += blockDim.x) {
+            const int g = v / LPG, kk = 2 * (v % LPG);
+            const uint32_t Lb = group_base(g);
+            const double x0 = srcd[2 * (Lb + offset_of(kk & (D - 1))) + (kk >> K)];
+            const double x1 = srcd[2 * (Lb + offset_of((kk + 1) & (D - 1))) + ((kk + 1) >> K)];
+            int eb = max((int)(((unsigned long long)__double_as_longlong(x0) >> 52) & 0x7FFu),
+                         (int)(((unsigned long long)__double_as_longlong(x1) >> 52) & 0x7FFu));
 #pragma unroll
-        for (int s = 0; s < kTcDigits; ++s)
-            *reinterpret_cast<uint32_t*>(planeA + (size_t)s * G * RH + (size_t)g * RH + kk) = pack_digits(d0[s], d1[s]);
+            for (int o = 1; o < LPG; o <<= 1) eb = max(eb, __shfl_xor_sync(0xffffffffu, eb, o));
+            if ((lane & (LPG - 1)) == 0) erow[g] = eb;
+            int d0[kTcDigits], d1[kTcDigits];
+            digits5(x0, eb, d0);
+            digits5(x1, eb, d1);
+#pragma unroll
+            for (int s = 0; s < kTcDigits; ++s)
+                *reinterpret_cast<uint32_t*>(planeA + (size_t)s * G * RH + (size_t)g * RH + kk) =
+                    pack_digits(d0[s], d1[s]);
+        }
     }
     __syncthreads();
 
@@ -373,18 +374,20 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
                         dstd[di] = srcd[di];
                         continue;
                     }
-                    const int base = er + ecol[jj] - 18;
+                    // sum_levels acc * 2^(-10 level) in double-float (exact powers
+                    // of two keep every term normal), then one scale by 2^(E_row + E_col - 18)
                     float sh = 0.f, sl = 0.f;
 #pragma unroll
                     for (int a = 0; a < 8; ++a) {
-                        const float f = scale_pow2(acc[a][n][h * 2 + c2], base - 10 * tc_level(a));
+                        const float f = acc[a][n][h * 2 + c2] * __int_as_float((127 - 10 * tc_level(a)) << 23);
                         const float t = sh + f;
                         const float bb = t - sh;
                         sl += (sh - (t - bb)) + (f - bb);
                         sh = t;
                     }
                     df_norm(sh, sl);
-                    dstd[di] = df_combine(sh, sl);
+                    const int sc = er + ecol[jj] - 18;
+                    dstd[di] = df_combine(scale_pow2(sh, sc), scale_pow2(sl, sc));
                 }
         }
     }
