@@ -237,6 +237,11 @@ __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]) : "r"(a));
 }
 
+__device__ __forceinline__ void ldsm_x2(uint32_t (&r)[2], const void* p) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x2.shared.b16 {%0,%1}, [%2];" : "=r"(r[0]), "=r"(r[1]) : "r"(a));
+}
+
 __device__ __forceinline__ void mma_f16(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
     asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
                  "{%0,%1,%2,%3};"
@@ -321,41 +326,43 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
     }
     __syncthreads();
 
-    // 3. MMA: warp task = (16 groups) x (16 output reals)
+    // 2. MMA: warp task = (16 groups) x (8 output reals)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int mtiles = G / 16;
-    constexpr int NP = KK / 16;
-    for (int task = warp; task < mtiles * NP; task += nwarps) {
-        const int mt = task / NP, np = task % NP;
-        float acc[8][2][4];
+    constexpr int NT = KK / 8;
+    for (int task = warp; task < mtiles * NT; task += nwarps) {
+        const int mt = task / NT, nt = task % NT;
+        float acc[8][4];
 #pragma unroll
         for (int a = 0; a < 8; ++a)
 #pragma unroll
-            for (int n = 0; n < 2; ++n)
+            for (int e = 0; e < 4; ++e) acc[a][e] = 0.f;
+        const int arow = mt * 16 + (lane & 7) + ((lane >> 3) & 1) * 8;
+        const int brow = nt * 8 + (lane & 7);
 #pragma unroll
-                for (int e = 0; e < 4; ++e) acc[a][n][e] = 0.f;
-#pragma unroll
-        for (int ks = 0; ks < KK / 16; ++ks) {
+        for (int kp = 0; kp < KK / 32 + (KK < 32 ? 1 : 0); ++kp) {
+            // two k16 steps per iteration (one when KK == 16): B fragments for
+            // both come from one ldmatrix.x4
             uint32_t af[kTcDigits][4];
-            const int arow = mt * 16 + (lane & 7) + ((lane >> 3) & 1) * 8;
-            const int acol = ks * 16 + (lane >> 4) * 8;
+            const int ks0 = kp * 2;
 #pragma unroll
-            for (int s = 0; s < kTcDigits; ++s) ldsm_x4(af[s], planeA + (size_t)s * G * RH + (size_t)arow * RH + acol);
-            const int brow = (np * 2 + (lane >> 4)) * 8 + (lane & 7);
-            const int bcol = ks * 16 + ((lane >> 3) & 1) * 8;
+            for (int half = 0; half < (KK < 32 ? 1 : 2); ++half) {
+                const int ks = ks0 + half;
+                const int acol = ks * 16 + (lane >> 4) * 8;
 #pragma unroll
-            for (int j = 0; j < kTcDigits; ++j) {
-                uint32_t bf[4];
-                ldsm_x4(bf, planeB + (size_t)j * KK * RH + (size_t)brow * RH + bcol);
+                for (int s = 0; s < kTcDigits; ++s)
+                    ldsm_x4(af[s], planeA + (size_t)s * G * RH + (size_t)arow * RH + acol);
+                const int bcol = ks * 16 + ((lane >> 3) & 1) * 8;
 #pragma unroll
-                for (int i = 0; i + j < kTcDigits; ++i) {
-                    const int a = tc_acc(i, j);
-                    mma_f16(acc[a][0], af[i], bf[0], bf[1]);
-                    mma_f16(acc[a][1], af[i], bf[2], bf[3]);
+                for (int j = 0; j < kTcDigits; ++j) {
+                    uint32_t bf[2];
+                    ldsm_x2(bf, planeB + (size_t)j * KK * RH + (size_t)brow * RH + bcol);
+#pragma unroll
+                    for (int i = 0; i + j < kTcDigits; ++i) mma_f16(acc[tc_acc(i, j)], af[i], bf[0], bf[1]);
                 }
             }
         }
-        // 4. epilogue: rows g0, g0 + 8; columns (np*2 + n)*8 + 2*tig + {0, 1}
+        // 3. epilogue: rows g0, g0 + 8; columns nt*8 + 2*tig + {0, 1}
         const int gid = lane >> 2, tig = lane & 3;
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
@@ -364,31 +371,29 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
             const bool ok = (Lb & op.ctrl_local) == op.ctrl_local;
             const int er = erow[g] - 1022;
 #pragma unroll
-            for (int n = 0; n < 2; ++n)
-#pragma unroll
-                for (int c2 = 0; c2 < 2; ++c2) {
-                    const int jj = (np * 2 + n) * 8 + tig * 2 + c2;
-                    const int r = jj & (D - 1), part = jj >> K;
-                    const size_t di = 2 * (size_t)(Lb + offset_of(r)) + part;
-                    if (!ok) {
-                        dstd[di] = srcd[di];
-                        continue;
-                    }
-                    // sum_levels acc * 2^(-10 level) in double-float (exact powers
-                    // of two keep every term normal), then one scale by 2^(E_row + E_col - 18)
-                    float sh = 0.f, sl = 0.f;
-#pragma unroll
-                    for (int a = 0; a < 8; ++a) {
-                        const float f = acc[a][n][h * 2 + c2] * __int_as_float((127 - 10 * tc_level(a)) << 23);
-                        const float t = sh + f;
-                        const float bb = t - sh;
-                        sl += (sh - (t - bb)) + (f - bb);
-                        sh = t;
-                    }
-                    df_norm(sh, sl);
-                    const int sc = er + ecol[jj] - 18;
-                    dstd[di] = df_combine(scale_pow2(sh, sc), scale_pow2(sl, sc));
+            for (int c2 = 0; c2 < 2; ++c2) {
+                const int jj = nt * 8 + tig * 2 + c2;
+                const int r = jj & (D - 1), part = jj >> K;
+                const size_t di = 2 * (size_t)(Lb + offset_of(r)) + part;
+                if (!ok) {
+                    dstd[di] = srcd[di];
+                    continue;
                 }
+                // sum_levels acc * 2^(-10 level) in double-float (exact powers
+                // of two keep every term normal), then one scale by 2^(E_row + E_col - 18)
+                float sh = 0.f, sl = 0.f;
+#pragma unroll
+                for (int a = 0; a < 8; ++a) {
+                    const float f = acc[a][h * 2 + c2] * __int_as_float((127 - 10 * tc_level(a)) << 23);
+                    const float t = sh + f;
+                    const float bb = t - sh;
+                    sl += (sh - (t - bb)) + (f - bb);
+                    sh = t;
+                }
+                df_norm(sh, sl);
+                const int sc = er + ecol[jj] - 18;
+                dstd[di] = df_combine(scale_pow2(sh, sc), scale_pow2(sl, sc));
+            }
         }
     }
 }
@@ -396,7 +401,7 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
 constexpr int kPassGPT = 4;
 
 template <class A>
-__global__ void __launch_bounds__(kThreads, A::kId == 4 ? 2 : 4) pass_kernel(typename A::store_t* __restrict__ state,
+__global__ void __launch_bounds__(kThreads, A::kId == 4 ? 3 : 4) pass_kernel(typename A::store_t* __restrict__ state,
                                                            const typename A::mat_t* __restrict__ mats,
                                                            const __grid_constant__ PassDesc d) {
     using C = typename A::comp_t;
@@ -802,7 +807,7 @@ size_t pass_smem_bytes(int arith, const PassDesc& d) {
     switch (arith) {
         case kArithF64: return pass_smem_t<ArithF64>(d);
         case kArithDF: return pass_smem_t<ArithDF>(d);
-        case kArithTC: return pass_smem_t<ArithDFRaw>(d);
+        case kArithTC: return d.tc_bytes ? pass_smem_t<ArithDFRaw>(d) : pass_smem_t<ArithDF>(d);
         default: return pass_smem_t<ArithF32>(d);
     }
 }
@@ -812,7 +817,10 @@ cudaError_t launch_pass(int arith, void* state, const void* mats, const PassDesc
         case kArithF64: return launch_pass_t<ArithF64>(state, mats, d, s);
         case kArithDF: return launch_pass_t<ArithDF>(state, mats, d, s);
         case kArithF32: return launch_pass_t<ArithF32>(state, mats, d, s);
-        case kArithTC: return launch_pass_t<ArithDFRaw>(state, mats, d, s);
+        // passes without tensor-core gates run the double-float kernel (same
+        // matrix format, fewer registers, more resident CTAs)
+        case kArithTC: return d.tc_bytes ? launch_pass_t<ArithDFRaw>(state, mats, d, s)
+                                         : launch_pass_t<ArithDF>(state, mats, d, s);
         default: return cudaErrorInvalidValue;
     }
 }
