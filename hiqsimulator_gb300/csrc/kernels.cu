@@ -184,8 +184,9 @@ __device__ __forceinline__ void apply_dense(const typename A::comp_t* __restrict
 //
 // A dense k-qubit gate (k = 3..5) on a tile of G = 2^(q-k) index groups is the
 // real GEMM  Y[G x 2D] = X[G x 2D] * B[2D x 2D],  D = 2^k, with X holding the
-// real then imaginary parts of each group's inputs and B the real form of the
-// gate ([Re M^T, Im M^T; -Im M^T, Re M^T]). Every entry of X is written as
+// interleaved real and imaginary parts of each group's inputs (column 2c + p)
+// and B the matching real form of the gate (B[2c][2r] = Re M_rc,
+// B[2c+1][2r] = -Im M_rc, B[2c][2r+1] = Im M_rc, B[2c+1][2r+1] = Re M_rc). Every entry of X is written as
 // 2^E_row * sum_i d_i 2^(-9-10i) with five signed digits |d_i| <= 512 (E_row
 // shared by the row), every entry of B likewise with E_col shared by the
 // column (digits computed on the host). Digits are exact in fp16, a product
@@ -269,8 +270,6 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
     const __half* planeB = reinterpret_cast<const __half*>(pool + 4 * KK);
     __half* planeA = reinterpret_cast<__half*>(scratch);
     int* erow = reinterpret_cast<int*>(scratch + (size_t)kTcDigits * G * RH * 2);
-    const double* srcd = reinterpret_cast<const double*>(src);
-    double* dstd = reinterpret_cast<double*>(dst);
 
     int ss[K];
     uint32_t bitv[K];
@@ -300,29 +299,45 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
         return o;
     };
 
-    // 1. digit planes of X: a group's 2D reals are handled by KK/2 consecutive
-    // lanes (two reals each); the row exponent is a max over those lanes.
-    {
-        constexpr int LPG = KK / 2;  // lanes per group (8, 16 or 32)
-        const int lane = threadIdx.x & 31;
-        for (int v = threadIdx.x; v < G * LPG; v += blockDim.x) {
-            const int g = v / LPG, kk = 2 * (v % LPG);
-            const uint32_t Lb = group_base(g);
-            const double x0 = srcd[2 * (Lb + offset_of(kk & (D - 1))) + (kk >> K)];
-            const double x1 = srcd[2 * (Lb + offset_of((kk + 1) & (D - 1))) + ((kk + 1) >> K)];
-            int eb = max((int)(((unsigned long long)__double_as_longlong(x0) >> 52) & 0x7FFu),
-                         (int)(((unsigned long long)__double_as_longlong(x1) >> 52) & 0x7FFu));
+    // 1. digit planes of X. Plane column 2c + p holds part p (0 re, 1 im) of
+    // input c. A work item is (group g, 4 consecutive inputs); consecutive
+    // threads take consecutive groups, so their tile reads are contiguous
+    // whenever tile bit 0 is not a target.
+    constexpr int CPI = 4;           // complex inputs per item
+    constexpr int NCH = D / CPI;     // items per group (D >= 8)
+    for (int g = threadIdx.x; g < G; g += blockDim.x) erow[g] = 0;
+    __syncthreads();
+    for (int it = threadIdx.x; it < G * NCH; it += blockDim.x) {
+        const int g = it % G, ch = it / G;
+        const uint32_t Lb = group_base(g);
+        int eb = 0;
 #pragma unroll
-            for (int o = 1; o < LPG; o <<= 1) eb = max(eb, __shfl_xor_sync(0xffffffffu, eb, o));
-            if ((lane & (LPG - 1)) == 0) erow[g] = eb;
-            int d0[kTcDigits], d1[kTcDigits];
-            digits5(x0, eb, d0);
-            digits5(x1, eb, d1);
-#pragma unroll
-            for (int s = 0; s < kTcDigits; ++s)
-                *reinterpret_cast<uint32_t*>(planeA + (size_t)s * G * RH + (size_t)g * RH + kk) =
-                    pack_digits(d0[s], d1[s]);
+        for (int u = 0; u < CPI; ++u) {
+            const double2 x = src[Lb + offset_of(ch * CPI + u)];
+            eb = max(eb, (int)(((unsigned long long)__double_as_longlong(x.x) >> 52) & 0x7FFu));
+            eb = max(eb, (int)(((unsigned long long)__double_as_longlong(x.y) >> 52) & 0x7FFu));
         }
+        if (eb) atomicMax(&erow[g], eb);
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < G * NCH; it += blockDim.x) {
+        const int g = it % G, ch = it / G;
+        const uint32_t Lb = group_base(g);
+        const int ebrow = erow[g];
+        uint32_t w[kTcDigits][CPI];
+#pragma unroll
+        for (int u = 0; u < CPI; ++u) {
+            const double2 x = src[Lb + offset_of(ch * CPI + u)];
+            int dr[kTcDigits], di[kTcDigits];
+            digits5(x.x, ebrow, dr);
+            digits5(x.y, ebrow, di);
+#pragma unroll
+            for (int sdx = 0; sdx < kTcDigits; ++sdx) w[sdx][u] = pack_digits(dr[sdx], di[sdx]);
+        }
+#pragma unroll
+        for (int sdx = 0; sdx < kTcDigits; ++sdx)
+            *reinterpret_cast<uint4*>(planeA + (size_t)sdx * G * RH + (size_t)g * RH + ch * 2 * CPI) =
+                make_uint4(w[sdx][0], w[sdx][1], w[sdx][2], w[sdx][3]);
     }
     __syncthreads();
 
@@ -362,23 +377,24 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
                 }
             }
         }
-        // 3. epilogue: rows g0, g0 + 8; columns nt*8 + 2*tig + {0, 1}
+        // 3. epilogue: rows g0 and g0 + 8; plane columns nt*8 + 2*tig + {0, 1}
+        // are the real and imaginary parts of output r = nt*4 + tig
         const int gid = lane >> 2, tig = lane & 3;
+        const int r = nt * 4 + tig;
+        const uint32_t orow = offset_of(r);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int g = mt * 16 + gid + h * 8;
             const uint32_t Lb = group_base(g);
-            const bool ok = (Lb & op.ctrl_local) == op.ctrl_local;
+            const uint32_t idx = Lb + orow;
+            if ((Lb & op.ctrl_local) != op.ctrl_local) {
+                dst[idx] = src[idx];
+                continue;
+            }
             const int er = erow[g] - 1022;
+            double outv[2];
 #pragma unroll
             for (int c2 = 0; c2 < 2; ++c2) {
-                const int jj = nt * 8 + tig * 2 + c2;
-                const int r = jj & (D - 1), part = jj >> K;
-                const size_t di = 2 * (size_t)(Lb + offset_of(r)) + part;
-                if (!ok) {
-                    dstd[di] = srcd[di];
-                    continue;
-                }
                 // sum_levels acc * 2^(-10 level) in double-float (exact powers
                 // of two keep every term normal), then one scale by 2^(E_row + E_col - 18)
                 float sh = 0.f, sl = 0.f;
@@ -391,9 +407,10 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
                     sh = t;
                 }
                 df_norm(sh, sl);
-                const int sc = er + ecol[jj] - 18;
-                dstd[di] = df_combine(scale_pow2(sh, sc), scale_pow2(sl, sc));
+                const int sc = er + ecol[nt * 8 + tig * 2 + c2] - 18;
+                outv[c2] = df_combine(scale_pow2(sh, sc), scale_pow2(sl, sc));
             }
+            dst[idx] = make_double2(outv[0], outv[1]);
         }
     }
 }

@@ -245,15 +245,17 @@ static void digits_host(double v, int ebmax, int* d) {
     d[0] = (int)X;
 }
 
-// Real form of a complex gate for the tensor-core path: rows kk of B are the
-// real (kk < D) then imaginary inputs, columns j the real (j < D) then
-// imaginary outputs.
+// Real form of a complex gate for the tensor-core path (B with Y = X B, X the
+// interleaved real and imaginary parts of a group's inputs).
 static void convert_tc(const GateOp& op, unsigned char* dst) {
     const int D = 1 << op.k, KK = 2 * D, RH = KK + 8;
+    // interleaved real form: row 2c + p_in is part p_in of input c, column
+    // 2r + p_out part p_out of output r
     auto bval = [&](int kk, int j) -> double {
-        const cplx m = op.m[(size_t)(j & (D - 1)) * D + (kk & (D - 1))];
-        if (kk < D) return j < D ? m.real() : m.imag();
-        return j < D ? -m.imag() : m.real();
+        const cplx m = op.m[(size_t)(j >> 1) * D + (kk >> 1)];
+        const int pin = kk & 1, pout = j & 1;
+        if (pin == 0) return pout == 0 ? m.real() : m.imag();
+        return pout == 0 ? -m.imag() : m.real();
     };
     int32_t* ecol = reinterpret_cast<int32_t*>(dst);
     uint16_t* planes = reinterpret_cast<uint16_t*>(dst + 4 * KK);
