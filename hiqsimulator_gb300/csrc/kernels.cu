@@ -225,12 +225,29 @@ __device__ __forceinline__ void digits5(double v, int ebrow, int (&d)[kTcDigits]
     d[0] = (int)X;
 }
 
-__device__ __forceinline__ float scale_pow2(float x, int s) {
-    if (s > 120) { x *= 0x1p120f; s -= 120; }
-    if (s < -120) { x *= 0x1p-120f; s += 120; }
-    if (s < -126) return 0.f;
-    return x * __int_as_float((s + 127) << 23);
+
+// S * 2^sc as the nearest double (ties away from zero), built from bits.
+__device__ __forceinline__ double fixed_to_double(long long S, int sc) {
+    if (S == 0) return 0.0;
+    const unsigned long long sgn = (S < 0) ? (1ULL << 63) : 0ULL;
+    unsigned long long a = (S < 0) ? (unsigned long long)(-S) : (unsigned long long)S;
+    int p = 63 - __clzll((long long)a);
+    unsigned long long m;
+    if (p <= 52) {
+        m = a << (52 - p);
+    } else {
+        const int sh = p - 52;
+        m = (a + (1ULL << (sh - 1))) >> sh;
+        if (m >> 53) {
+            m >>= 1;
+            ++p;
+        }
+    }
+    const int biased = p + sc + 1023;
+    if (biased <= 0) return __longlong_as_double((long long)sgn);
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)biased << 52) | (m & 0xFFFFFFFFFFFFFULL)));
 }
+
 
 __device__ __forceinline__ void ldsm_x4(uint32_t (&r)[4], const void* p) {
     const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
@@ -395,20 +412,18 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
             double outv[2];
 #pragma unroll
             for (int c2 = 0; c2 < 2; ++c2) {
-                // sum_levels acc * 2^(-10 level) in double-float (exact powers
-                // of two keep every term normal), then one scale by 2^(E_row + E_col - 18)
-                float sh = 0.f, sl = 0.f;
-#pragma unroll
-                for (int a = 0; a < 8; ++a) {
-                    const float f = acc[a][h * 2 + c2] * __int_as_float((127 - 10 * tc_level(a)) << 23);
-                    const float t = sh + f;
-                    const float bb = t - sh;
-                    sl += (sh - (t - bb)) + (f - bb);
-                    sh = t;
-                }
-                df_norm(sh, sl);
-                const int sc = er + ecol[nt * 8 + tig * 2 + c2] - 18;
-                outv[c2] = df_combine(scale_pow2(sh, sc), scale_pow2(sl, sc));
+                // accumulators hold integers: level sums as one fixed-point
+                // int64 S = L0 2^30 + L1 2^20 + L2 2^10 + L3 + L4 2^-10 (< 2^55),
+                // value = S * 2^(E_row + E_col - 48)
+                const int e = h * 2 + c2;
+                const long long L0 = __float2int_rn(acc[0][e]);
+                const long long L1 = (long long)__float2int_rn(acc[1][e]) + __float2int_rn(acc[2][e]);
+                const long long L2 =
+                    (long long)__float2int_rn(acc[3][e]) + __float2int_rn(acc[4][e]) + __float2int_rn(acc[5][e]);
+                const long long L3 = __float2int_rn(acc[6][e]);
+                const long long L4 = __float2int_rn(acc[7][e]);
+                const long long S = (L0 << 30) + (L1 << 20) + (L2 << 10) + L3 + (L4 >> 10);
+                outv[c2] = fixed_to_double(S, er + ecol[nt * 8 + tig * 2 + c2] - 48);
             }
             dst[idx] = make_double2(outv[0], outv[1]);
         }

@@ -136,7 +136,12 @@ std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& o
         std::memset(&d, 0, sizeof(d));
         // tile: the pass's targets plus at least 4 low positions, 2^10 amplitudes
         // at least (enough index groups for every thread), at most 2^max_tile_bits
-        int q = std::min(n, std::max(popc64(tset), std::min(max_tile_bits, std::max(popc64(tset) + 4, 10))));
+        // tensor-core passes use 2^9-amplitude tiles (16 index groups for a 5-qubit
+        // gate) so that three CTAs fit on an SM next to the gate's digit planes
+        bool has_tc = false;
+        for (size_t o = i; o < j; ++o) has_tc = has_tc || tc_candidate(arith, ops[o]);
+        const int base_q = has_tc ? 9 : 10;
+        int q = std::min(n, std::max(popc64(tset), std::min(max_tile_bits, std::max(popc64(tset) + 4, base_q))));
         // keep the pass within one CTA's shared memory: shrink the tile (not
         // below the targets), then give up tensor-core gates if still too big
         bool allow_tc = true;
