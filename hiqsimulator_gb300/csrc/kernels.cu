@@ -205,26 +205,44 @@ __device__ __forceinline__ uint32_t pack_digits(int d0, int d1) {
 }
 
 // Digits of v relative to the row's largest biased exponent ebrow
-// (|v| < 2^(ebrow - 1022)), most significant first.
+// (|v| < 2^(ebrow - 1022)), most significant first: X = round(|v| 2^(49-E_row))
+// < 2^49 is cut into five 10-bit fields, which are balanced into [-512, 511]
+// (the top one into [-512, 512]) with carries, then given v's sign.
 __device__ __forceinline__ void digits5(double v, int ebrow, int (&d)[kTcDigits]) {
     const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-    const int eb = (int)((u >> 52) & 0x7FFu);
-    long long X = 0;
-    if (eb != 0) {
-        const long long M = (long long)((u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52));
-        const int sh = 4 + ebrow - eb;  // X = round(v * 2^(49 - E_row)) = round(M / 2^sh)
-        if (sh < 62) X = (M + (1LL << (sh - 1))) >> sh;
-        if (u >> 63) X = -X;
+    const uint32_t hi = (uint32_t)(u >> 32);
+    const int eb = (int)((hi >> 20) & 0x7FFu);
+    unsigned long long a = 0;
+    const int sh = 4 + ebrow - eb;  // >= 4
+    if (eb != 0 && sh < 62) {
+        const unsigned long long M = (u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+        a = (M + (1ULL << (sh - 1))) >> sh;
     }
-#pragma unroll
-    for (int i = kTcDigits - 1; i >= 1; --i) {
-        const int dd = (int)((X + 512) & 1023) - 512;
-        d[i] = dd;
-        X = (X - dd) >> 10;
-    }
-    d[0] = (int)X;
+    const uint32_t alo = (uint32_t)a, ahi = (uint32_t)(a >> 32);
+    int r4 = (int)(alo & 1023u);
+    int r3 = (int)((alo >> 10) & 1023u);
+    int r2 = (int)((alo >> 20) & 1023u);
+    int r1 = (int)(__funnelshift_r(alo, ahi, 30) & 1023u);
+    int r0 = (int)(ahi >> 8);
+    int c = (r4 + 512) >> 10;
+    r4 -= c << 10;
+    r3 += c;
+    c = (r3 + 512) >> 10;
+    r3 -= c << 10;
+    r2 += c;
+    c = (r2 + 512) >> 10;
+    r2 -= c << 10;
+    r1 += c;
+    c = (r1 + 512) >> 10;
+    r1 -= c << 10;
+    r0 += c;
+    const int sg = (int)(hi >> 31) ? -1 : 0;  // negate all digits for negative v
+    d[0] = (r0 ^ sg) - sg;
+    d[1] = (r1 ^ sg) - sg;
+    d[2] = (r2 ^ sg) - sg;
+    d[3] = (r3 ^ sg) - sg;
+    d[4] = (r4 ^ sg) - sg;
 }
-
 
 // S * 2^sc as the nearest double (ties away from zero), built from bits.
 __device__ __forceinline__ double fixed_to_double(long long S, int sc) {
@@ -320,8 +338,8 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
     // input c. A work item is (group g, 4 consecutive inputs); consecutive
     // threads take consecutive groups, so their tile reads are contiguous
     // whenever tile bit 0 is not a target.
-    constexpr int CPI = 4;           // complex inputs per item
-    constexpr int NCH = D / CPI;     // items per group (D >= 8)
+    constexpr int CPI = 2;           // complex inputs per item
+    constexpr int NCH = D / CPI;     // items per group
     for (int g = threadIdx.x; g < G; g += blockDim.x) erow[g] = 0;
     __syncthreads();
     for (int it = threadIdx.x; it < G * NCH; it += blockDim.x) {
@@ -353,8 +371,8 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
         }
 #pragma unroll
         for (int sdx = 0; sdx < kTcDigits; ++sdx)
-            *reinterpret_cast<uint4*>(planeA + (size_t)sdx * G * RH + (size_t)g * RH + ch * 2 * CPI) =
-                make_uint4(w[sdx][0], w[sdx][1], w[sdx][2], w[sdx][3]);
+            *reinterpret_cast<uint2*>(planeA + (size_t)sdx * G * RH + (size_t)g * RH + ch * 2 * CPI) =
+                make_uint2(w[sdx][0], w[sdx][1]);
     }
     __syncthreads();
 

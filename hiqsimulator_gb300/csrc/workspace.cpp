@@ -230,24 +230,29 @@ static int biased_exponent(double v) {
 }
 
 // The five balanced base-2^10 digits of v relative to the biased exponent
-// ebmax of its column (same rule as the device-side digits of the state).
+// ebmax of its column (same rule as the device-side digits of the state):
+// a = round(|v| 2^(49 - E)) cut into 10-bit fields, balanced into [-512, 511]
+// with carries upward, then given v's sign.
 static void digits_host(double v, int ebmax, int* d) {
     uint64_t u;
     std::memcpy(&u, &v, 8);
     const int eb = (int)((u >> 52) & 0x7FF);
-    long long X = 0;
-    if (eb != 0) {
-        const long long M = (long long)((u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52));
-        const int sh = 4 + ebmax - eb;
-        if (sh < 62) X = (M + (1LL << (sh - 1))) >> sh;
-        if (u >> 63) X = -X;
+    uint64_t a = 0;
+    const int sh = 4 + ebmax - eb;
+    if (eb != 0 && sh < 62) {
+        const uint64_t M = (u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+        a = (M + (1ULL << (sh - 1))) >> sh;
     }
+    int r[kTcDigits];
+    for (int i = 0; i < kTcDigits; ++i) r[kTcDigits - 1 - i] = (int)((a >> (10 * i)) & 1023u);
+    r[0] = (int)(a >> 40);
     for (int i = kTcDigits - 1; i >= 1; --i) {
-        const int dd = (int)((X + 512) & 1023) - 512;
-        d[i] = dd;
-        X = (X - dd) >> 10;
+        const int c = (r[i] + 512) >> 10;
+        r[i] -= c << 10;
+        r[i - 1] += c;
     }
-    d[0] = (int)X;
+    const bool neg = (u >> 63) != 0;
+    for (int i = 0; i < kTcDigits; ++i) d[i] = neg ? -r[i] : r[i];
 }
 
 // Real form of a complex gate for the tensor-core path (B with Y = X B, X the
