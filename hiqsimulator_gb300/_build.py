@@ -20,8 +20,8 @@ NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 CU_SOURCES = ["kernels.cu", "noalloc.cu"]
-CXX_SOURCES = ["fusion.cpp", "workspace.cpp", "engine.cpp", "scheduler.cpp", "capi.cpp"]
-HEADERS = ["hqs_desc.h", "hqs_kernels.h", "hqs_arith.cuh", "fusion.h", "workspace.h", "engine.h"]
+CXX_SOURCES = ["fusion.cpp", "workspace.cpp", "engine.cpp", "scheduler.cpp", "server.cpp", "capi.cpp"]
+HEADERS = ["hqs_desc.h", "hqs_kernels.h", "hqs_arith.cuh", "fusion.h", "workspace.h", "engine.h", "server.h"]
 
 LIB = os.path.join(PKG, "libhqs.so")
 EXT = sysconfig.get_config_var("EXT_SUFFIX") or ".so"

@@ -9,6 +9,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "server.h"
 #include "workspace.h"
 
 namespace hqs {
@@ -21,6 +22,12 @@ struct hqs_sim {
     hqs::Engine* eng = nullptr;
     std::string err;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
+};
+
+struct hqs_server {
+    hqs::Server* srv = nullptr;
+    std::string err;
+    std::vector<hqs::ServerResult> pending;  // completed, not yet returned
 };
 
 struct hqs_ws {
@@ -368,6 +375,103 @@ int hqs_greedy_schedule(int ngates, const int64_t* tgt, const int* toff, const i
         if (nc < 0) throw std::runtime_error("CalcPos(): scheduling with 64 or more qubits is not yet supported");
         *nclusters = nc;
     });
+}
+
+// ----------------------------------------------------------- server
+
+int hqs_server_create(int precision, int arith, uint64_t budget_bytes, int max_active, int cluster_size,
+                      hqs_server** out) {
+    if (!out) return HQS_ERR_INVALID;
+    *out = nullptr;
+    hqs_server* s = new (std::nothrow) hqs_server();
+    if (!s) return HQS_ERR_MEMORY;
+    const int rc = guarded(g_err, [&]() {
+        need(precision == HQS_C128 || precision == HQS_C64, "precision must be HQS_C128 or HQS_C64");
+        s->srv = new hqs::Server(precision, arith, budget_bytes, max_active, cluster_size);
+    });
+    if (rc != HQS_OK) {
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return HQS_OK;
+}
+
+void hqs_server_destroy(hqs_server* srv) {
+    if (!srv) return;
+    delete srv->srv;
+    delete srv;
+}
+
+const char* hqs_server_last_error(const hqs_server* srv) { return srv ? srv->err.c_str() : g_err.c_str(); }
+
+int hqs_server_submit(hqs_server* srv, int n, int ngates, const int* ntgt, const int* tgt, const int* nctl,
+                      const int* ctl, const double* mats, int kind, double rnd, size_t nterms, const uint64_t* px,
+                      const uint64_t* py, const uint64_t* pz, const double* coefs, uint64_t* id_out) {
+    if (!srv) return HQS_ERR_INVALID;
+    return guarded(srv->err, [&]() {
+        need(ngates >= 0 && (ngates == 0 || (ntgt && nctl && mats)), "null gate arrays");
+        need(kind >= HQS_RESULT_AMPLITUDE0 && kind <= HQS_RESULT_EXPECTATION, "unknown result kind");
+        std::vector<hqs::ServerGate> gates(ngates);
+        size_t ti = 0, ci = 0, mi = 0;
+        for (int g = 0; g < ngates; ++g) {
+            need(ntgt[g] >= 0 && ntgt[g] <= 10 && nctl[g] >= 0, "bad gate size");
+            gates[g].targets.assign(tgt + ti, tgt + ti + ntgt[g]);
+            gates[g].ctrls.assign(ctl + ci, ctl + ci + nctl[g]);
+            ti += ntgt[g];
+            ci += nctl[g];
+            const size_t dim = (size_t)1 << ntgt[g];
+            gates[g].m.resize(dim * dim);
+            std::memcpy(static_cast<void*>(gates[g].m.data()), mats + 2 * mi, dim * dim * sizeof(hqs::cplx));
+            mi += dim * dim;
+        }
+        std::vector<uint64_t> x, y, z;
+        std::vector<hqs::cplx> c;
+        if (kind == HQS_RESULT_EXPECTATION) {
+            need(nterms == 0 || (px && py && pz && coefs), "null Pauli arrays");
+            x.assign(px, px + nterms);
+            y.assign(py, py + nterms);
+            z.assign(pz, pz + nterms);
+            for (size_t t = 0; t < nterms; ++t) c.emplace_back(coefs[2 * t], coefs[2 * t + 1]);
+        }
+        const uint64_t id = srv->srv->submit(n, gates, kind, rnd, x, y, z, c);
+        if (id_out) *id_out = id;
+    });
+}
+
+int hqs_server_step(hqs_server* srv, hqs_server_result* out, size_t cap, size_t* n) {
+    if (!srv) return HQS_ERR_INVALID;
+    return guarded(srv->err, [&]() {
+        if (srv->pending.empty() || cap == 0) {
+            std::vector<hqs::ServerResult> r = srv->srv->step();
+            srv->pending.insert(srv->pending.end(), r.begin(), r.end());
+        }
+        size_t k = std::min(cap, srv->pending.size());
+        for (size_t i = 0; i < k; ++i) {
+            const hqs::ServerResult& r = srv->pending[i];
+            out[i].id = r.id;
+            out[i].kind = r.kind;
+            out[i].value_re = r.value_re;
+            out[i].value_im = r.value_im;
+            out[i].sample = r.sample;
+            out[i].submit_s = r.submit_s;
+            out[i].admit_s = r.admit_s;
+            out[i].done_s = r.done_s;
+            out[i].passes = r.passes;
+        }
+        srv->pending.erase(srv->pending.begin(), srv->pending.begin() + k);
+        if (n) *n = k;
+    });
+}
+
+int hqs_server_info(const hqs_server* srv, uint64_t out[5]) {
+    if (!srv || !out) return HQS_ERR_INVALID;
+    out[0] = srv->srv->queued();
+    out[1] = srv->srv->active();
+    out[2] = srv->srv->bytes_in_use();
+    out[3] = srv->srv->rounds();
+    out[4] = srv->srv->launches() + 0 * srv->pending.size();
+    return HQS_OK;
 }
 
 // ----------------------------------------------------------- kernel level

@@ -25,6 +25,19 @@ int device_sm_count();
 cudaError_t launch_pass(int arith, void* state, const void* mats, const PassDesc& d, cudaStream_t s);
 size_t pass_smem_bytes(int arith, const PassDesc& d);
 
+// One entry of a batched launch: a pass over one state. Device-resident.
+struct BatchItem {
+    void* state;
+    const void* mats;      // device pointer to the pass's matrix pool
+    uint64_t tile_begin;   // first global tile index of this item
+    PassDesc desc;
+};
+// Run every item's pass in one launch (total_tiles = sum of the items' tiles,
+// smem = the largest pass_smem_bytes of the items). With arith == kArithTC,
+// tc selects the tensor-core kernel (needed when any item has TC gates).
+cudaError_t launch_batch(int arith, bool tc, const BatchItem* d_items, int nitems, uint64_t total_tiles, size_t smem,
+                         cudaStream_t s);
+
 // Sum of |a_i|^2 over indices with (i & mask) == val.
 cudaError_t reduce_probability(int arith, const void* state, int n, uint64_t mask, uint64_t val,
                                ReduceScratch& rs, cudaStream_t s, double* out);

@@ -450,87 +450,140 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
 
 constexpr int kPassGPT = 4;
 
+// Shared-memory layout of a pass (host and device agree through pass_smem_t):
+// [matrix pool][tile A][tile B][high-bit offsets][16-aligned tensor-core scratch]
 template <class A>
-__global__ void __launch_bounds__(kThreads, A::kId == 4 ? 3 : 4) pass_kernel(typename A::store_t* __restrict__ state,
-                                                           const typename A::mat_t* __restrict__ mats,
-                                                           const __grid_constant__ PassDesc d) {
-    using C = typename A::comp_t;
-    using M = typename A::mat_t;
-    extern __shared__ __align__(16) unsigned char smem[];
-    M* smat = reinterpret_cast<M*>(smem);
-    const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(M) + 15) & ~(size_t)15;
-    const int Q = 1 << d.q;
-    C* bufA = reinterpret_cast<C*>(smem + mat_bytes);
-    C* bufB = bufA + Q;
-    uint64_t* hoff = reinterpret_cast<uint64_t*>(bufB + Q);
-    const int nh = d.q - d.w;
-    const uint32_t lowmask = (1u << d.w) - 1u;
-    // tensor-core scratch, 16-byte aligned for ldmatrix
-    unsigned char* tcs = smem + ((mat_bytes + 2 * sizeof(C) * (size_t)Q + sizeof(uint64_t) * ((size_t)1 << nh) + 15) &
-                                 ~(size_t)15);
+struct PassSmem {
+    typename A::mat_t* smat;
+    typename A::comp_t* bufA;
+    typename A::comp_t* bufB;
+    uint64_t* hoff;
+    unsigned char* tcs;
+    __device__ __forceinline__ PassSmem(unsigned char* smem, const PassDesc& d) {
+        const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(typename A::mat_t) + 15) & ~(size_t)15;
+        const size_t Q = (size_t)1 << d.q;
+        smat = reinterpret_cast<typename A::mat_t*>(smem);
+        bufA = reinterpret_cast<typename A::comp_t*>(smem + mat_bytes);
+        bufB = bufA + Q;
+        hoff = reinterpret_cast<uint64_t*>(bufB + Q);
+        tcs = smem + ((mat_bytes + 2 * sizeof(typename A::comp_t) * Q + sizeof(uint64_t) * ((size_t)1 << (d.q - d.w)) +
+                       15) & ~(size_t)15);
+    }
+};
 
-    for (uint32_t i = threadIdx.x; i < d.mat_elems; i += blockDim.x) smat[i] = mats[i];
+// Stage a pass's matrices and tile offsets into shared memory.
+template <class A>
+__device__ __forceinline__ void pass_setup(const PassSmem<A>& sm, const PassDesc& d,
+                                           const typename A::mat_t* __restrict__ mats) {
+    const int nh = d.q - d.w;
+    for (uint32_t i = threadIdx.x; i < d.mat_elems; i += blockDim.x) sm.smat[i] = mats[i];
     for (int j = threadIdx.x; j < (1 << nh); j += blockDim.x) {
         uint64_t o = 0;
         for (int b = 0; b < nh; ++b)
             if ((j >> b) & 1) o |= 1ULL << d.tile_pos[d.w + b];
-        hoff[j] = o;
+        sm.hoff[j] = o;
     }
     __syncthreads();
+}
 
-    const uint64_t ntiles = 1ULL << (d.n - d.nins);
-    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-        uint64_t base = t;
-        for (int i = 0; i < d.nins; ++i) base = insert_zero(base, d.ins_pos[i]);
-        base |= d.fixed_mask;
-        for (int L = threadIdx.x; L < Q; L += blockDim.x)
-            bufA[L] = A::to_comp(state[base + hoff[L >> d.w] + (L & lowmask)]);
-        __syncthreads();
-        C* src = bufA;
-        C* dst = bufB;
-        for (int oi = 0; oi < d.nops; ++oi) {
-            const OpDesc& op = d.ops[oi];
-            if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
-            if (op.k == 0) {
-                apply_scalar<A>(src, smat[op.mat_off], Q);
-                __syncthreads();
-                continue;
-            }
-            if (op.diag) {
-                apply_diag<A>(src, smat + op.mat_off, op, Q);
-                __syncthreads();
-                continue;
-            }
-            if constexpr (A::kId == 4) {
-                if (op.tc) {
-                    const unsigned char* pool = reinterpret_cast<const unsigned char*>(smat + op.mat_off);
-                    switch (op.k) {
-                        case 3: apply_tc<3>(src, dst, pool, op, d.q, tcs); break;
-                        case 4: apply_tc<4>(src, dst, pool, op, d.q, tcs); break;
-                        default: apply_tc<5>(src, dst, pool, op, d.q, tcs); break;
-                    }
-                    __syncthreads();
-                    C* tmp = src;
-                    src = dst;
-                    dst = tmp;
-                    continue;
-                }
-            }
-            switch (op.k) {
-                case 1: apply_dense<A, 1, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
-                case 2: apply_dense<A, 2, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
-                case 3: apply_dense<A, 3, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
-                case 4: apply_dense<A, 4, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
-                default: apply_dense<A, 5, kPassGPT>(src, dst, smat + op.mat_off, op, d.q); break;
-            }
+// One tile of a pass: load, apply the pass's gates in order, store.
+template <class A>
+__device__ __forceinline__ void pass_tile(typename A::store_t* __restrict__ state, const PassDesc& d,
+                                          const PassSmem<A>& sm, uint64_t t) {
+    using C = typename A::comp_t;
+    const int Q = 1 << d.q;
+    const uint32_t lowmask = (1u << d.w) - 1u;
+    uint64_t base = t;
+    for (int i = 0; i < d.nins; ++i) base = insert_zero(base, d.ins_pos[i]);
+    base |= d.fixed_mask;
+    for (int L = threadIdx.x; L < Q; L += blockDim.x)
+        sm.bufA[L] = A::to_comp(state[base + sm.hoff[L >> d.w] + (L & lowmask)]);
+    __syncthreads();
+    C* src = sm.bufA;
+    C* dst = sm.bufB;
+    for (int oi = 0; oi < d.nops; ++oi) {
+        const OpDesc& op = d.ops[oi];
+        if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
+        if (op.k == 0) {
+            apply_scalar<A>(src, sm.smat[op.mat_off], Q);
             __syncthreads();
-            C* tmp = src;
-            src = dst;
-            dst = tmp;
+            continue;
         }
-        for (int L = threadIdx.x; L < Q; L += blockDim.x)
-            state[base + hoff[L >> d.w] + (L & lowmask)] = A::from_comp(src[L]);
+        if (op.diag) {
+            apply_diag<A>(src, sm.smat + op.mat_off, op, Q);
+            __syncthreads();
+            continue;
+        }
+        if constexpr (A::kId == 4) {
+            if (op.tc) {
+                const unsigned char* pool = reinterpret_cast<const unsigned char*>(sm.smat + op.mat_off);
+                switch (op.k) {
+                    case 3: apply_tc<3>(src, dst, pool, op, d.q, sm.tcs); break;
+                    case 4: apply_tc<4>(src, dst, pool, op, d.q, sm.tcs); break;
+                    default: apply_tc<5>(src, dst, pool, op, d.q, sm.tcs); break;
+                }
+                __syncthreads();
+                C* tmp = src;
+                src = dst;
+                dst = tmp;
+                continue;
+            }
+        }
+        switch (op.k) {
+            case 1: apply_dense<A, 1, kPassGPT>(src, dst, sm.smat + op.mat_off, op, d.q); break;
+            case 2: apply_dense<A, 2, kPassGPT>(src, dst, sm.smat + op.mat_off, op, d.q); break;
+            case 3: apply_dense<A, 3, kPassGPT>(src, dst, sm.smat + op.mat_off, op, d.q); break;
+            case 4: apply_dense<A, 4, kPassGPT>(src, dst, sm.smat + op.mat_off, op, d.q); break;
+            default: apply_dense<A, 5, kPassGPT>(src, dst, sm.smat + op.mat_off, op, d.q); break;
+        }
         __syncthreads();
+        C* tmp = src;
+        src = dst;
+        dst = tmp;
+    }
+    for (int L = threadIdx.x; L < Q; L += blockDim.x)
+        state[base + sm.hoff[L >> d.w] + (L & lowmask)] = A::from_comp(src[L]);
+    __syncthreads();
+}
+
+template <class A>
+__global__ void __launch_bounds__(kThreads, A::kId == 4 ? 3 : 4) pass_kernel(typename A::store_t* __restrict__ state,
+                                                                             const typename A::mat_t* __restrict__ mats,
+                                                                             const __grid_constant__ PassDesc d) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const PassSmem<A> sm(smem, d);
+    pass_setup<A>(sm, d, mats);
+    const uint64_t ntiles = 1ULL << (d.n - d.nins);
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) pass_tile<A>(state, d, sm, t);
+}
+
+// Many passes (one per independent state) in one launch: global tile index T
+// belongs to the item whose tile range contains it; each CTA walks its tiles
+// in increasing T and re-stages the pass when it crosses into a new item.
+template <class A>
+__global__ void __launch_bounds__(kThreads, A::kId == 4 ? 3 : 4) batch_pass_kernel(const BatchItem* __restrict__ items,
+                                                                                   int nitems, uint64_t total_tiles) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ PassDesc sd;
+    int cur = -1;
+    for (uint64_t T = blockIdx.x; T < total_tiles; T += gridDim.x) {
+        int lo = 0, hi = nitems - 1;
+        while (lo < hi) {  // last item with tile_begin <= T
+            const int mid = (lo + hi + 1) >> 1;
+            if (items[mid].tile_begin <= T) lo = mid;
+            else hi = mid - 1;
+        }
+        if (lo != cur) {
+            __syncthreads();
+            const uint32_t* srcw = reinterpret_cast<const uint32_t*>(&items[lo].desc);
+            uint32_t* dstw = reinterpret_cast<uint32_t*>(&sd);
+            for (int w = threadIdx.x; w < (int)(sizeof(PassDesc) / 4); w += blockDim.x) dstw[w] = srcw[w];
+            __syncthreads();
+            cur = lo;
+            pass_setup<A>(PassSmem<A>(smem, sd), sd, reinterpret_cast<const typename A::mat_t*>(items[lo].mats));
+        }
+        pass_tile<A>(reinterpret_cast<typename A::store_t*>(items[lo].state), sd, PassSmem<A>(smem, sd),
+                     T - items[lo].tile_begin);
     }
 }
 
@@ -539,6 +592,22 @@ size_t pass_smem_t(const PassDesc& d) {
     const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(typename A::mat_t) + 15) & ~(size_t)15;
     return ((mat_bytes + 2 * (sizeof(typename A::comp_t) << d.q) + sizeof(uint64_t) * (1u << (d.q - d.w)) + 15) &
             ~(size_t)15) + d.tc_bytes;
+}
+
+template <class A>
+cudaError_t launch_batch_t(const BatchItem* d_items, int nitems, uint64_t total_tiles, size_t smem, cudaStream_t s) {
+    auto kern = batch_pass_kernel<A>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    uint64_t grid = (uint64_t)device_sm_count() * per_sm;
+    if (grid > total_tiles) grid = total_tiles;
+    if (grid == 0) return cudaSuccess;
+    kern<<<(unsigned)grid, kThreads, smem, s>>>(d_items, nitems, total_tiles);
+    return cudaGetLastError();
 }
 
 template <class A>
@@ -871,6 +940,18 @@ cudaError_t launch_pass(int arith, void* state, const void* mats, const PassDesc
         // matrix format, fewer registers, more resident CTAs)
         case kArithTC: return d.tc_bytes ? launch_pass_t<ArithDFRaw>(state, mats, d, s)
                                          : launch_pass_t<ArithDF>(state, mats, d, s);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_batch(int arith, bool tc, const BatchItem* d_items, int nitems, uint64_t total_tiles, size_t smem,
+                         cudaStream_t s) {
+    switch (arith) {
+        case kArithF64: return launch_batch_t<ArithF64>(d_items, nitems, total_tiles, smem, s);
+        case kArithDF: return launch_batch_t<ArithDF>(d_items, nitems, total_tiles, smem, s);
+        case kArithF32: return launch_batch_t<ArithF32>(d_items, nitems, total_tiles, smem, s);
+        case kArithTC: return tc ? launch_batch_t<ArithDFRaw>(d_items, nitems, total_tiles, smem, s)
+                                 : launch_batch_t<ArithDF>(d_items, nitems, total_tiles, smem, s);
         default: return cudaErrorInvalidValue;
     }
 }

@@ -1,0 +1,324 @@
+#include "server.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <stdexcept>
+
+namespace hqs {
+
+namespace {
+
+// A fused gate (DenseGate over ids 0..n-1, ids == positions) as a GateOp, the
+// way SimulatorMPI::Run dispatches it (SimulatorMPI.cpp:470-524).
+bool to_gate_op(const DenseGate& g, const std::vector<int64_t>& ctrls, GateOp& op) {
+    op = GateOp();
+    op.k = (int)g.ids.size();
+    if (op.k > kMaxK) throw std::runtime_error("server: a fused gate acts on more than 5 qubits");
+    if (op.k == 0) {
+        if (g.m[0] == cplx(1.0, 0.0)) return false;
+        op.m = {g.m[0]};
+        return true;
+    }
+    for (int j = 0; j < op.k; ++j) op.pos[j] = (int)g.ids[j];
+    for (int64_t c : ctrls) op.ctrl_mask |= 1ULL << c;
+    op.diag = g.diag;
+    if (g.diag) {
+        op.m.resize(g.dim);
+        for (int r = 0; r < g.dim; ++r) op.m[r] = g.m[(size_t)r * g.dim + r];
+    } else {
+        op.m = g.m;
+    }
+    return true;
+}
+
+}  // namespace
+
+Server::Server(int precision, int arith, uint64_t budget_bytes, int max_active, int cluster_size)
+    : precision_(precision),
+      arith_(arith),
+      max_active_(std::max(1, max_active)),
+      cluster_(std::max(1, std::min(cluster_size, kMaxK))),
+      budget_(budget_bytes) {
+    if (arith_ == 0) arith_ = precision_ == 1 ? kArithF32 : kArithTC;
+    if ((precision_ == 1) != (arith_ == kArithF32)) throw std::invalid_argument("server: precision/arith mismatch");
+    for (int i = 0; i < 2; ++i) cuda_check(cudaEventCreateWithFlags(&staging_done_[i], cudaEventDisableTiming), "cudaEventCreate");
+    cuda_check(cudaMalloc(&blocks_dev_, sizeof(double) << 15), "cudaMalloc(blocks)");
+    cuda_check(cudaMallocHost(&blocks_host_, sizeof(double) << 15), "cudaMallocHost(blocks)");
+    t0_ = 0;
+    t0_ = now();
+}
+
+Server::~Server() {
+    cudaStreamSynchronize(ws_.stream());
+    for (auto& r : active_)
+        if (r.state) cudaFreeAsync(r.state, ws_.stream());
+    cudaStreamSynchronize(ws_.stream());
+    for (int i = 0; i < 2; ++i) {
+        cudaFreeHost(staging_[i]);
+        cudaFree(dev_[i]);
+        cudaEventDestroy(staging_done_[i]);
+    }
+    cudaFree(blocks_dev_);
+    cudaFreeHost(blocks_host_);
+}
+
+double Server::now() const {
+    using namespace std::chrono;
+    return duration<double>(steady_clock::now().time_since_epoch()).count() - t0_;
+}
+
+uint64_t Server::submit(int n, const std::vector<ServerGate>& gates, int kind, double rnd,
+                        const std::vector<uint64_t>& pauli_x, const std::vector<uint64_t>& pauli_y,
+                        const std::vector<uint64_t>& pauli_z, const std::vector<cplx>& pauli_coef) {
+    if (n < 1 || n > 40) throw std::invalid_argument("server: qubit count out of range");
+    Req r;
+    r.id = next_id_++;
+    r.n = n;
+    r.kind = kind;
+    r.rnd = rnd;
+    r.px = pauli_x;
+    r.py = pauli_y;
+    r.pz = pauli_z;
+    r.pc = pauli_coef;
+    r.bytes = ((uint64_t)1 << n) * (precision_ == 1 ? 8 : 16);
+    r.submit_s = now();
+    // Sequential greedy fusion: gates join the current fused gate while the
+    // union of their qubits stays within cluster_; controlled gates too large
+    // to fuse go alone with their controls as a control mask.
+    Fusion fu;
+    uint64_t cur = 0;
+    auto flush = [&]() {
+        if (fu.empty()) return;
+        DenseGate g;
+        std::vector<int64_t> ctrls;
+        fu.perform(g, ctrls);
+        GateOp op;
+        if (to_gate_op(g, ctrls, op)) r.ops.push_back(std::move(op));
+        fu.clear();
+        cur = 0;
+    };
+    for (const auto& sg : gates) {
+        const int dim = 1 << sg.targets.size();
+        if ((size_t)dim * dim != sg.m.size()) throw std::invalid_argument("server: matrix size does not match targets");
+        uint64_t q = 0;
+        for (int t : sg.targets) {
+            if (t < 0 || t >= n) throw std::invalid_argument("server: target out of range");
+            q |= 1ULL << t;
+        }
+        for (int c : sg.ctrls) {
+            if (c < 0 || c >= n) throw std::invalid_argument("server: control out of range");
+            q |= 1ULL << c;
+        }
+        DenseGate g;
+        g.dim = dim;
+        g.m = sg.m;
+        g.diag = is_diagonal(sg.m, dim);
+        g.ids.assign(sg.targets.begin(), sg.targets.end());
+        std::vector<int64_t> cs(sg.ctrls.begin(), sg.ctrls.end());
+        if ((int)(sg.targets.size() + sg.ctrls.size()) > cluster_) {
+            flush();
+            fu.insert(std::move(g), cs);
+            flush();
+            continue;
+        }
+        if (__builtin_popcountll(cur | q) > cluster_) flush();
+        add_controls(g, cs);
+        fu.insert(std::move(g), {});
+        cur |= q;
+    }
+    flush();
+    queue_.push_back(std::move(r));
+    return queue_.back().id;
+}
+
+ServerResult Server::finish(Req& r) {
+    ServerResult res{};
+    res.id = r.id;
+    res.kind = r.kind;
+    res.submit_s = r.submit_s;
+    res.admit_s = r.admit_s;
+    res.passes = r.passes;
+    cudaStream_t s = ws_.stream();
+    const size_t eb = precision_ == 1 ? 8 : 16;
+    if (r.kind == kResultAmplitude0) {
+        if (eb == 8) {
+            float v[2];
+            cuda_check(cudaMemcpyAsync(v, r.state, 8, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+            cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+            res.value_re = v[0];
+            res.value_im = v[1];
+        } else {
+            double v[2];
+            cuda_check(cudaMemcpyAsync(v, r.state, 16, cudaMemcpyDeviceToHost, s), "cudaMemcpyAsync");
+            cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+            res.value_re = v[0];
+            res.value_im = v[1];
+        }
+    } else if (r.kind == kResultSample) {
+        const uint64_t N = 1ULL << r.n;
+        const uint64_t nb = std::min<uint64_t>(N, 1ULL << 15);
+        cuda_check(block_sums(arith_, r.state, r.n, nb, blocks_dev_, s), "block_sums");
+        cuda_check(cudaMemcpyAsync(blocks_host_, blocks_dev_, nb * sizeof(double), cudaMemcpyDeviceToHost, s),
+                   "cudaMemcpyAsync");
+        cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        std::partial_sum(blocks_host_, blocks_host_ + nb, blocks_host_);
+        uint64_t i = std::lower_bound(blocks_host_, blocks_host_ + nb, r.rnd) - blocks_host_;
+        if (i == nb) i = nb - 1;
+        const uint64_t K = N / nb;
+        scan_.resize(K);
+        if (eb == 8) {
+            std::vector<float> tmp(2 * K);
+            cuda_check(cudaMemcpyAsync(tmp.data(), static_cast<unsigned char*>(r.state) + i * K * 8, K * 8,
+                                       cudaMemcpyDeviceToHost, s),
+                       "cudaMemcpyAsync");
+            cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+            for (uint64_t j = 0; j < K; ++j) scan_[j] = cplx(tmp[2 * j], tmp[2 * j + 1]);
+        } else {
+            cuda_check(cudaMemcpyAsync(scan_.data(), static_cast<unsigned char*>(r.state) + i * K * 16, K * 16,
+                                       cudaMemcpyDeviceToHost, s),
+                       "cudaMemcpyAsync");
+            cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+        }
+        double shift = i > 0 ? blocks_host_[i - 1] : 0.0;
+        uint64_t k = i * K;
+        for (uint64_t j = 0; j < K; ++j, ++k) {
+            shift += std::norm(scan_[j]);
+            if (shift >= r.rnd) break;
+        }
+        res.sample = std::min(k, N - 1);
+    } else {
+        const size_t T = r.px.size();
+        std::vector<unsigned char> blob(T * (3 * 8 + 16) + 16);
+        std::memcpy(blob.data(), r.px.data(), T * 8);
+        std::memcpy(blob.data() + T * 8, r.py.data(), T * 8);
+        std::memcpy(blob.data() + 2 * T * 8, r.pz.data(), T * 8);
+        double* co = reinterpret_cast<double*>(blob.data() + 3 * T * 8);
+        for (size_t t = 0; t < T; ++t) {
+            co[2 * t] = r.pc[t].real();
+            co[2 * t + 1] = r.pc[t].imag();
+        }
+        double out = 0.0;
+        if (T > 0) {
+            const unsigned char* d = static_cast<const unsigned char*>(ws_.upload(blob.data(), blob.size()));
+            cuda_check(reduce_pauli_expectation(arith_, r.state, r.n, (int)T, (const uint64_t*)d,
+                                                (const uint64_t*)(d + T * 8), (const uint64_t*)(d + 2 * T * 8),
+                                                (const double*)(d + 3 * T * 8), ws_.reduce(), s, &out),
+                       "reduce_pauli_expectation");
+        }
+        res.value_re = out;
+    }
+    cuda_check(cudaFreeAsync(r.state, s), "cudaFreeAsync");
+    r.state = nullptr;
+    bytes_in_use_ -= r.bytes;
+    res.done_s = now();
+    return res;
+}
+
+std::vector<ServerResult> Server::step() {
+    std::vector<ServerResult> done;
+    cudaStream_t s = ws_.stream();
+    // 1. finish circuits whose last pass was launched in an earlier round
+    std::vector<Req> keep;
+    keep.reserve(active_.size());
+    for (auto& r : active_) {
+        if (r.next >= r.ops.size()) done.push_back(finish(r));
+        else keep.push_back(std::move(r));
+    }
+    active_.swap(keep);
+    // 2. admit waiting requests in arrival order while memory and slots allow
+    while (!queue_.empty() && (int)active_.size() < max_active_ && bytes_in_use_ + queue_.front().bytes <= budget_) {
+        Req r = std::move(queue_.front());
+        queue_.pop_front();
+        cuda_check(cudaMallocAsync(&r.state, r.bytes, s), "cudaMallocAsync(state)");
+        cuda_check(cudaMemsetAsync(r.state, 0, r.bytes, s), "cudaMemsetAsync");
+        cuda_check(fill_value(arith_, r.state, 1, 1.0, 0.0, s), "fill_value");
+        bytes_in_use_ += r.bytes;
+        r.admit_s = now();
+        active_.push_back(std::move(r));
+    }
+    if (!queue_.empty() && active_.empty() && queue_.front().bytes > budget_)
+        throw std::runtime_error("server: a request needs more HBM than the admission budget");
+    // 3. plan the next pass of every resident circuit
+    struct Planned {
+        Req* r;
+        PassPlan plan;
+        size_t first, nops;
+    };
+    std::vector<Planned> tc_items, plain_items;
+    for (auto& r : active_) {
+        if (r.next >= r.ops.size()) continue;
+        const size_t window = std::min<size_t>(r.ops.size() - r.next, kMaxOpsPerPass);
+        std::vector<GateOp> slice(r.ops.begin() + r.next, r.ops.begin() + r.next + window);
+        std::vector<size_t> first;
+        std::vector<PassPlan> plans = plan_passes(r.n, arith_, slice, 11, 16, &first);
+        Planned p{&r, plans[0], r.next, (size_t)plans[0].desc.nops};
+        (plans[0].desc.tc_bytes ? tc_items : plain_items).push_back(p);
+        r.next += p.nops;
+        ++r.passes;
+    }
+    // 4. stage descriptors + matrices, one copy, one launch per kernel kind
+    auto launch = [&](std::vector<Planned>& items, bool tc) {
+        if (items.empty()) return;
+        const size_t head = ((items.size() * sizeof(BatchItem)) + 255) & ~(size_t)255;
+        size_t total = head;
+        for (auto& it : items) total += pass_pool_bytes(arith_, it.plan.desc);
+        const int f = flip_;
+        flip_ ^= 1;
+        cuda_check(cudaEventSynchronize(staging_done_[f]), "cudaEventSynchronize");
+        if (staging_bytes_[f] < total) {
+            cudaFreeHost(staging_[f]);
+            staging_[f] = nullptr;
+            staging_bytes_[f] = 0;
+            cuda_check(cudaMallocHost(&staging_[f], total * 2), "cudaMallocHost(staging)");
+            staging_bytes_[f] = total * 2;
+        }
+        if (dev_bytes_[f] < total) {
+            cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+            cudaFree(dev_[f]);
+            dev_[f] = nullptr;
+            dev_bytes_[f] = 0;
+            cuda_check(cudaMalloc(&dev_[f], total * 2), "cudaMalloc(batch)");
+            dev_bytes_[f] = total * 2;
+        }
+        unsigned char* host = static_cast<unsigned char*>(staging_[f]);
+        unsigned char* dev = static_cast<unsigned char*>(dev_[f]);
+        BatchItem* bi = reinterpret_cast<BatchItem*>(host);
+        size_t off = head;
+        uint64_t tiles = 0;
+        size_t smem = 0;
+        for (size_t i = 0; i < items.size(); ++i) {
+            const PassDesc& d = items[i].plan.desc;
+            bi[i].state = items[i].r->state;
+            bi[i].mats = dev + off;
+            bi[i].tile_begin = tiles;
+            bi[i].desc = d;
+            write_pass_pool(arith_, d, items[i].r->ops.data() + items[i].first, host + off);
+            off += pass_pool_bytes(arith_, d);
+            tiles += 1ULL << (d.n - d.nins);
+            smem = std::max(smem, pass_smem_bytes(tc ? kArithTC : (arith_ == kArithTC ? kArithDF : arith_), d));
+        }
+        cuda_check(cudaMemcpyAsync(dev, host, total, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(batch)");
+        cuda_check(cudaEventRecord(staging_done_[f], s), "cudaEventRecord");
+        cuda_check(launch_batch(arith_, tc, reinterpret_cast<const BatchItem*>(dev), (int)items.size(), tiles, smem, s),
+                   "launch_batch");
+        ++launches_;
+    };
+    launch(tc_items, true);
+    launch(plain_items, false);
+    ++rounds_;
+    return done;
+}
+
+std::vector<ServerResult> Server::drain() {
+    std::vector<ServerResult> all;
+    while (!queue_.empty() || !active_.empty()) {
+        std::vector<ServerResult> d = step();
+        all.insert(all.end(), d.begin(), d.end());
+    }
+    return all;
+}
+
+}  // namespace hqs

@@ -320,6 +320,20 @@ static void convert_matrix(int arith, const GateOp& op, unsigned char* dst) {
     }
 }
 
+size_t pass_pool_bytes(int arith, const PassDesc& d) {
+    return ((size_t)d.mat_elems * Workspace::mat_elem_bytes(arith) + 255) & ~(size_t)255;
+}
+
+void write_pass_pool(int arith, const PassDesc& d, const GateOp* ops, unsigned char* dst) {
+    size_t off = 0;
+    for (int o = 0; o < d.nops; ++o) {
+        const bool tc = d.ops[o].tc != 0;
+        if (tc) convert_tc(ops[o], dst + off);
+        else convert_matrix(arith, ops[o], dst + off);
+        off += pool_elems(arith, ops[o], tc) * Workspace::mat_elem_bytes(arith);
+    }
+}
+
 uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits,
                               int max_ops, uint64_t* passes_out) {
     if (ops.empty()) return 0;

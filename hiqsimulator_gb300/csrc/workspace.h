@@ -97,6 +97,11 @@ private:
     cudaEvent_t take_event();
 };
 
+// Bytes of a planned pass's matrix pool and the pool itself (ops are the
+// pass's gates, in order), in the arithmetic's element format.
+size_t pass_pool_bytes(int arith, const PassDesc& d);
+void write_pass_pool(int arith, const PassDesc& d, const GateOp* ops, unsigned char* dst);
+
 // Build the pass descriptors for ops (exposed for host-side tests of the planner).
 std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits, int max_ops,
                                   std::vector<size_t>* op_first = nullptr);

@@ -167,6 +167,47 @@ int hqs_greedy_schedule(int ngates, const int64_t* tgt, const int* toff, const i
                         int* nclusters);
 
 /* ------------------------------------------------------------------------
+ * Batched circuit server (no reference counterpart): many independent
+ * circuits resident in HBM, admitted in arrival order against a byte budget
+ * (2^n x bytes per amplitude) and advanced together, one fused pass per
+ * circuit per round in a single batched launch.
+ * ------------------------------------------------------------------------ */
+typedef struct hqs_server hqs_server;
+
+#define HQS_RESULT_AMPLITUDE0 0  /* <0...0|psi> */
+#define HQS_RESULT_SAMPLE 1      /* one full-register sample for the given uniform draw */
+#define HQS_RESULT_EXPECTATION 2 /* sum_t Re(c_t <psi|P_t|psi>) */
+
+typedef struct {
+    uint64_t id;
+    int kind;
+    double value_re, value_im; /* amplitude, or the expectation in value_re */
+    uint64_t sample;           /* basis index for HQS_RESULT_SAMPLE */
+    double submit_s, admit_s, done_s;
+    uint32_t passes;
+} hqs_server_result;
+
+/* precision HQS_C128 / HQS_C64; arith as for hqs_sim_create; budget_bytes:
+ * HBM for resident states; max_active: resident circuits at most;
+ * cluster_size: gates are fused while their qubits fit (<= 5). */
+int hqs_server_create(int precision, int arith, uint64_t budget_bytes, int max_active, int cluster_size,
+                      hqs_server** out);
+void hqs_server_destroy(hqs_server* srv);
+const char* hqs_server_last_error(const hqs_server* srv);
+/* Queue a circuit on n qubits: gate g has ntgt[g] targets and nctl[g]
+ * controls (qubit indices 0..n-1, concatenated in tgt / ctl) and a
+ * 2^ntgt x 2^ntgt row-major complex128 matrix (concatenated in mats). For
+ * HQS_RESULT_EXPECTATION, nterms Pauli terms are given as x / y / z bit masks
+ * over qubit indices and complex coefficients. */
+int hqs_server_submit(hqs_server* srv, int n, int ngates, const int* ntgt, const int* tgt, const int* nctl,
+                      const int* ctl, const double* mats, int kind, double rnd, size_t nterms, const uint64_t* px,
+                      const uint64_t* py, const uint64_t* pz, const double* coefs, uint64_t* id_out);
+/* One round; completed results go to out (cap entries), their count to *n. */
+int hqs_server_step(hqs_server* srv, hqs_server_result* out, size_t cap, size_t* n);
+/* queued, resident, bytes in use, rounds, launches */
+int hqs_server_info(const hqs_server* srv, uint64_t out[5]);
+
+/* ------------------------------------------------------------------------
  * Kernel-level API on device memory (one fused gate / reduction per call).
  * state: device pointer to 2^n amplitudes (complex128 for HQS_ARITH_F64/DF,
  * complex64 for HQS_ARITH_F32). stream: a cudaStream_t or NULL. Calls are
