@@ -470,7 +470,7 @@ int hqs_server_info(const hqs_server* srv, uint64_t out[5]) {
     out[1] = srv->srv->active();
     out[2] = srv->srv->bytes_in_use();
     out[3] = srv->srv->rounds();
-    out[4] = srv->srv->launches() + 0 * srv->pending.size();
+    out[4] = srv->srv->launches();
     return HQS_OK;
 }
 
