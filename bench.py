@@ -193,6 +193,65 @@ def cpu_sample(cmds, clusters, max_gates, budget_s):
         done, t_total)
 
 
+def serving_report(args):
+    """Config-4-style serving (smaller count): Poisson arrivals of circuits with
+    n ~ U{10..22}, depth ~ U{10..60}; batched continuous serving against the
+    same server running one circuit per launch."""
+    from hiqsimulator_gb300 import serving
+    out = {"circuits": args.serve, "budget_bytes": int(150e9),
+           "workload": "n~U{10..22}, depth~U{10..60} random layers; 30% sample, 20% 8-term <H>, 50% <0|psi>"}
+    circuits = serving.serving_workload(2024, args.serve)
+    for prec in ("c128", "c64"):
+        rep = {}
+        for rate in args.serve_rates:
+            arr = serving.poisson_arrivals(2024, len(circuits), rate)
+            res_b, st_b = serving.serve(circuits, arr, precision=prec, budget_bytes=150e9)
+            entry = {"batched": st_b}
+            if prec == "c128" and rate == args.serve_rates[0]:
+                res_p, st_p = serving.serve(circuits, arr, precision=prec, budget_bytes=150e9, max_active=1)
+                same = all((res_b[i]["value_re"], res_b[i]["value_im"], res_b[i]["sample"]) ==
+                           (res_p[i]["value_re"], res_p[i]["value_im"], res_p[i]["sample"]) for i in res_b)
+                entry["one_circuit_per_launch"] = st_p
+                entry["results_identical"] = bool(same)
+                entry["speedup_circuits_per_s"] = st_b["circuits_per_s"] / st_p["circuits_per_s"]
+            rep["rate_%g_per_s" % rate] = entry
+            log("serving %s rate %g: %.0f circuits/s p50 %.1f ms p99 %.1f ms" % (
+                prec, rate, st_b["circuits_per_s"], st_b["p50_ms"], st_b["p99_ms"]))
+        out[prec] = rep
+    return out
+
+
+def precision_report(qubits=24, layers=40):
+    """Config-3-style precision check: brickwork of Haar U(4) (fusion off, one
+    pass per gate) in complex64 (FP32) and complex128 (tensor-core mode); the
+    complex64 state against the complex128 one as fidelity and max error, and
+    the time of each."""
+    import hiqsimulator_gb300 as hqs
+    from hiqsimulator_gb300 import circuits
+    gates = circuits.brickwork(2024, list(range(qubits)), layers)
+    cmds = circuits.fusion_off_stream(gates)
+    out = {"workload": "%dq brickwork, %d layers of Haar U(4), fusion off" % (qubits, layers)}
+    states = {}
+    for prec in ("c128", "c64"):
+        sim = hqs.SimulatorMPI(7, qubits, 5, prec)
+        sim.set_pass_limits(defer=16)
+        sim.allocate_qureg(list(range(qubits)), 0)
+        sim.synchronize()
+        sim.timer_start()
+        circuits.replay(sim, cmds)
+        ms = sim.timer_stop()
+        _, states[prec] = sim.cheat_local_numpy()
+        out[prec + "_ms"] = ms
+        del sim
+    a, b = states["c128"], states["c64"]
+    out["fidelity_c64_vs_c128"] = float(abs(np.vdot(a, b)) ** 2)
+    out["max_abs_error_c64"] = float(np.max(np.abs(a - b)))
+    out["speedup_c64_over_c128"] = out["c128_ms"] / out["c64_ms"]
+    log("precision: fidelity %.9f max err %.2e, c128 %.0f ms, c64 %.0f ms" % (
+        out["fidelity_c64_vs_c128"], out["max_abs_error_c64"], out["c128_ms"], out["c64_ms"]))
+    return out
+
+
 def run_reference(args, dist):
     if dist.rank != 0:
         return 0
@@ -296,6 +355,9 @@ def run_ours(args, dist):
         v, threads, desc = cpu_sample(cmds, clusters, max_gates=2, budget_s=20.0)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
 
+    serv = serving_report(args) if (dist.rank == 0 and args.serve > 0) else None
+    prec = precision_report() if (dist.rank == 0 and not args.no_precision) else None
+
     if dist.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -307,7 +369,7 @@ def run_ours(args, dist):
                            "state_bytes": 16 << N_QUBITS, "l2": "inputs larger than L2 (16 GiB state)",
                            "parallelism": "replicas" if dist.ws > 1 else "single GPU"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk}
+                "clocks": clk, "serving": serv, "precision": prec}
         print(json.dumps(line), flush=True)
     return 0
 
@@ -323,6 +385,9 @@ def main():
     ap.add_argument("--defer", type=int, default=8, help="fused gates queued before the engine launches")
     ap.add_argument("--qubits", type=int, default=30, help="state size (30 is the benchmark configuration)")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--serve", type=int, default=400, help="circuits in the serving run (0 skips it)")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[4000.0, 400.0])
+    ap.add_argument("--no-precision", action="store_true")
     args = ap.parse_args()
     global N_QUBITS
     N_QUBITS = args.qubits
