@@ -205,7 +205,8 @@ def serving_report(args):
         rep = {}
         for rate in args.serve_rates:
             arr = serving.poisson_arrivals(2024, len(circuits), rate)
-            res_b, st_b = serving.serve(circuits, arr, precision=prec, budget_bytes=150e9)
+            res_b, st_b = serving.serve(circuits, arr, precision=prec, budget_bytes=150e9,
+                                        max_active=args.serve_slots)
             entry = {"batched": st_b}
             if prec == "c128" and rate == args.serve_rates[0]:
                 res_p, st_p = serving.serve(circuits, arr, precision=prec, budget_bytes=150e9, max_active=1)
@@ -244,7 +245,7 @@ def precision_report(qubits=24, layers=40):
         out[prec + "_ms"] = ms
         del sim
     a, b = states["c128"], states["c64"]
-    out["fidelity_c64_vs_c128"] = float(abs(np.vdot(a, b)) ** 2)
+    out["fidelity_c64_vs_c128"] = float(abs(np.vdot(a, b)) ** 2 / (np.vdot(a, a).real * np.vdot(b, b).real))
     out["max_abs_error_c64"] = float(np.max(np.abs(a - b)))
     out["speedup_c64_over_c128"] = out["c128_ms"] / out["c64_ms"]
     log("precision: fidelity %.9f max err %.2e, c128 %.0f ms, c64 %.0f ms" % (
@@ -387,6 +388,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--serve", type=int, default=400, help="circuits in the serving run (0 skips it)")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[4000.0, 400.0])
+    ap.add_argument("--serve-slots", type=int, default=32, help="resident circuits at most while serving")
     ap.add_argument("--no-precision", action="store_true")
     args = ap.parse_args()
     global N_QUBITS

@@ -566,7 +566,11 @@ __global__ void __launch_bounds__(kThreads, A::kId == 4 ? 3 : 4) batch_pass_kern
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ PassDesc sd;
     int cur = -1;
-    for (uint64_t T = blockIdx.x; T < total_tiles; T += gridDim.x) {
+    // contiguous chunk of tiles per CTA: few item switches (each re-stages the
+    // item's matrices) and neighbouring tiles of one state stay together
+    const uint64_t chunk = (total_tiles + gridDim.x - 1) / gridDim.x;
+    const uint64_t t_end = min(total_tiles, (uint64_t)(blockIdx.x + 1) * chunk);
+    for (uint64_t T = (uint64_t)blockIdx.x * chunk; T < t_end; ++T) {
         int lo = 0, hi = nitems - 1;
         while (lo < hi) {  // last item with tile_begin <= T
             const int mid = (lo + hi + 1) >> 1;
