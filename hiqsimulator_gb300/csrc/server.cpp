@@ -130,6 +130,10 @@ uint64_t Server::submit(int n, const std::vector<ServerGate>& gates, int kind, d
         cur |= q;
     }
     flush();
+    // digit planes of tensor-core-sized gates once, not every round
+    if (arith_ == kArithTC)
+        for (auto& op : r.ops)
+            if (op.k >= 3 && !op.diag) op.tc_pool = make_tc_pool(op);
     queue_.push_back(std::move(r));
     return queue_.back().id;
 }
@@ -251,9 +255,8 @@ std::vector<ServerResult> Server::step() {
     for (auto& r : active_) {
         if (r.next >= r.ops.size()) continue;
         const size_t window = std::min<size_t>(r.ops.size() - r.next, kMaxOpsPerPass);
-        std::vector<GateOp> slice(r.ops.begin() + r.next, r.ops.begin() + r.next + window);
         std::vector<size_t> first;
-        std::vector<PassPlan> plans = plan_passes(r.n, arith_, slice, 11, 16, &first);
+        std::vector<PassPlan> plans = plan_passes(r.n, arith_, r.ops.data() + r.next, window, 11, 16, &first, 1);
         Planned p{&r, plans[0], r.next, (size_t)plans[0].desc.nops};
         (plans[0].desc.tc_bytes ? tc_items : plain_items).push_back(p);
         r.next += p.nops;

@@ -107,8 +107,8 @@ static size_t pool_elems(int arith, const GateOp& op, bool tc) {
     return op.m.size();
 }
 
-std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits, int max_ops,
-                                  std::vector<size_t>* op_first) {
+std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t nops, int max_tile_bits, int max_ops,
+                                  std::vector<size_t>* op_first, size_t max_passes) {
     const size_t melem = Workspace::mat_elem_bytes(arith);
     const size_t store = (arith == kArithF32) ? 8 : 16;
     const size_t mat_budget = 64 * 1024;
@@ -116,11 +116,11 @@ std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& o
     max_ops = std::max(1, std::min(max_ops, kMaxOpsPerPass));
     std::vector<PassPlan> plans;
     size_t i = 0, pool_off = 0;
-    while (i < ops.size()) {
+    while (i < nops && plans.size() < max_passes) {
         uint64_t tset = 0;
         size_t mbytes = 0, j = i;
         if (op_first) op_first->push_back(i);
-        while (j < ops.size() && (int)(j - i) < max_ops) {
+        while (j < nops && (int)(j - i) < max_ops) {
             const GateOp& op = ops[j];
             uint64_t tm = 0;
             for (int t = 0; t < op.k; ++t) tm |= 1ULL << op.pos[t];
@@ -324,11 +324,18 @@ size_t pass_pool_bytes(int arith, const PassDesc& d) {
     return ((size_t)d.mat_elems * Workspace::mat_elem_bytes(arith) + 255) & ~(size_t)255;
 }
 
+std::shared_ptr<const std::vector<unsigned char>> make_tc_pool(const GateOp& op) {
+    auto v = std::make_shared<std::vector<unsigned char>>(tc_pool_bytes(op.k));
+    convert_tc(op, v->data());
+    return v;
+}
+
 void write_pass_pool(int arith, const PassDesc& d, const GateOp* ops, unsigned char* dst) {
     size_t off = 0;
     for (int o = 0; o < d.nops; ++o) {
         const bool tc = d.ops[o].tc != 0;
-        if (tc) convert_tc(ops[o], dst + off);
+        if (tc && ops[o].tc_pool) std::memcpy(dst + off, ops[o].tc_pool->data(), ops[o].tc_pool->size());
+        else if (tc) convert_tc(ops[o], dst + off);
         else convert_matrix(arith, ops[o], dst + off);
         off += pool_elems(arith, ops[o], tc) * Workspace::mat_elem_bytes(arith);
     }

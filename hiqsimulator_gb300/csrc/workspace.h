@@ -6,6 +6,7 @@
 
 #include <complex>
 #include <cstdint>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -24,6 +25,9 @@ struct GateOp {
     int pos[kMaxK] = {0, 0, 0, 0, 0};  // state position of matrix bit j
     uint64_t ctrl_mask = 0;    // state positions that must be 1
     std::vector<cplx> m;       // dense: dim*dim row-major; diag: dim entries; k == 0: 1 entry
+    // tensor-core pool bytes of this gate, computed once when the gate is
+    // reused across many flushes (the batched server); empty: computed on use
+    std::shared_ptr<const std::vector<unsigned char>> tc_pool;
 };
 
 struct PassPlan {
@@ -103,7 +107,13 @@ size_t pass_pool_bytes(int arith, const PassDesc& d);
 void write_pass_pool(int arith, const PassDesc& d, const GateOp* ops, unsigned char* dst);
 
 // Build the pass descriptors for ops (exposed for host-side tests of the planner).
-std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits, int max_ops,
-                                  std::vector<size_t>* op_first = nullptr);
+std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t nops, int max_tile_bits, int max_ops,
+                                  std::vector<size_t>* op_first = nullptr, size_t max_passes = SIZE_MAX);
+inline std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits,
+                                         int max_ops, std::vector<size_t>* op_first = nullptr) {
+    return plan_passes(n, arith, ops.data(), ops.size(), max_tile_bits, max_ops, op_first);
+}
+// The tensor-core pool bytes of a dense gate (k >= 3), for GateOp::tc_pool.
+std::shared_ptr<const std::vector<unsigned char>> make_tc_pool(const GateOp& op);
 
 }  // namespace hqs
