@@ -566,11 +566,12 @@ __global__ void __launch_bounds__(kThreads, A::kId == 4 ? 3 : 4) batch_pass_kern
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ PassDesc sd;
     int cur = -1;
-    // contiguous chunk of tiles per CTA: few item switches (each re-stages the
-    // item's matrices) and neighbouring tiles of one state stay together
-    const uint64_t chunk = (total_tiles + gridDim.x - 1) / gridDim.x;
-    const uint64_t t_end = min(total_tiles, (uint64_t)(blockIdx.x + 1) * chunk);
-    for (uint64_t T = (uint64_t)blockIdx.x * chunk; T < t_end; ++T) {
+    // runs of 8 consecutive tiles, dealt round-robin to the CTAs: a CTA
+    // re-stages an item's matrices at most once per run, and every CTA sees
+    // a mix of cheap and expensive items
+    constexpr uint64_t kRun = 8;
+    for (uint64_t T0 = (uint64_t)blockIdx.x * kRun; T0 < total_tiles; T0 += (uint64_t)gridDim.x * kRun)
+    for (uint64_t T = T0; T < min(total_tiles, T0 + kRun); ++T) {
         int lo = 0, hi = nitems - 1;
         while (lo < hi) {  // last item with tile_begin <= T
             const int mid = (lo + hi + 1) >> 1;
@@ -608,7 +609,8 @@ cudaError_t launch_batch_t(const BatchItem* d_items, int nitems, uint64_t total_
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     uint64_t grid = (uint64_t)device_sm_count() * per_sm;
-    if (grid > total_tiles) grid = total_tiles;
+    const uint64_t runs = (total_tiles + 7) / 8;
+    if (grid > runs) grid = runs;
     if (grid == 0) return cudaSuccess;
     kern<<<(unsigned)grid, kThreads, smem, s>>>(d_items, nitems, total_tiles);
     return cudaGetLastError();

@@ -249,25 +249,35 @@ std::vector<ServerResult> Server::step() {
     struct Planned {
         Req* r;
         PassPlan plan;
-        size_t first, nops;
+        size_t first;
+        bool tc;
+        size_t smem;
     };
-    std::vector<Planned> tc_items, plain_items;
+    std::vector<Planned> planned;
     for (auto& r : active_) {
         if (r.next >= r.ops.size()) continue;
         const size_t window = std::min<size_t>(r.ops.size() - r.next, kMaxOpsPerPass);
         std::vector<size_t> first;
-        std::vector<PassPlan> plans = plan_passes(r.n, arith_, r.ops.data() + r.next, window, 11, 16, &first, 1);
-        Planned p{&r, plans[0], r.next, (size_t)plans[0].desc.nops};
-        (plans[0].desc.tc_bytes ? tc_items : plain_items).push_back(p);
-        r.next += p.nops;
+        std::vector<PassPlan> plans = plan_passes(r.n, arith_, r.ops.data() + r.next, window, 10, 16, &first, 1);
+        Planned p{&r, plans[0], r.next, plans[0].desc.tc_bytes != 0, 0};
+        p.smem = pass_smem_bytes(p.tc ? kArithTC : (arith_ == kArithTC ? kArithDF : arith_), p.plan.desc);
+        r.next += (size_t)plans[0].desc.nops;
         ++r.passes;
+        planned.push_back(p);
     }
-    // 4. stage descriptors + matrices, one copy, one launch per kernel kind
-    auto launch = [&](std::vector<Planned>& items, bool tc) {
-        if (items.empty()) return;
-        const size_t head = ((items.size() * sizeof(BatchItem)) + 255) & ~(size_t)255;
+    // 4. one launch per (kernel, shared-memory class): a launch runs at the
+    // occupancy of its largest pass, so passes are grouped by footprint
+    auto smem_class = [](size_t b) { return b <= 56 * 1024 ? 0 : b <= 75 * 1024 ? 1 : b <= 112 * 1024 ? 2 : 3; };
+    std::stable_sort(planned.begin(), planned.end(), [&](const Planned& a, const Planned& b) {
+        if (a.tc != b.tc) return a.tc > b.tc;
+        return smem_class(a.smem) < smem_class(b.smem);
+    });
+    auto launch = [&](size_t lo, size_t hi) {
+        const bool tc = planned[lo].tc;
+        const size_t nitems = hi - lo;
+        const size_t head = ((nitems * sizeof(BatchItem)) + 255) & ~(size_t)255;
         size_t total = head;
-        for (auto& it : items) total += pass_pool_bytes(arith_, it.plan.desc);
+        for (size_t i = lo; i < hi; ++i) total += pass_pool_bytes(arith_, planned[i].plan.desc);
         const int f = flip_;
         flip_ ^= 1;
         cuda_check(cudaEventSynchronize(staging_done_[f]), "cudaEventSynchronize");
@@ -292,25 +302,32 @@ std::vector<ServerResult> Server::step() {
         size_t off = head;
         uint64_t tiles = 0;
         size_t smem = 0;
-        for (size_t i = 0; i < items.size(); ++i) {
-            const PassDesc& d = items[i].plan.desc;
-            bi[i].state = items[i].r->state;
-            bi[i].mats = dev + off;
-            bi[i].tile_begin = tiles;
-            bi[i].desc = d;
-            write_pass_pool(arith_, d, items[i].r->ops.data() + items[i].first, host + off);
+        for (size_t i = lo; i < hi; ++i) {
+            const PassDesc& d = planned[i].plan.desc;
+            BatchItem& b = bi[i - lo];
+            b.state = planned[i].r->state;
+            b.mats = dev + off;
+            b.tile_begin = tiles;
+            b.desc = d;
+            write_pass_pool(arith_, d, planned[i].r->ops.data() + planned[i].first, host + off);
             off += pass_pool_bytes(arith_, d);
             tiles += 1ULL << (d.n - d.nins);
-            smem = std::max(smem, pass_smem_bytes(tc ? kArithTC : (arith_ == kArithTC ? kArithDF : arith_), d));
+            smem = std::max(smem, planned[i].smem);
         }
         cuda_check(cudaMemcpyAsync(dev, host, total, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(batch)");
         cuda_check(cudaEventRecord(staging_done_[f], s), "cudaEventRecord");
-        cuda_check(launch_batch(arith_, tc, reinterpret_cast<const BatchItem*>(dev), (int)items.size(), tiles, smem, s),
+        cuda_check(launch_batch(arith_, tc, reinterpret_cast<const BatchItem*>(dev), (int)nitems, tiles, smem, s),
                    "launch_batch");
         ++launches_;
     };
-    launch(tc_items, true);
-    launch(plain_items, false);
+    for (size_t lo = 0; lo < planned.size();) {
+        size_t hi = lo + 1;
+        while (hi < planned.size() && planned[hi].tc == planned[lo].tc &&
+               smem_class(planned[hi].smem) == smem_class(planned[lo].smem))
+            ++hi;
+        launch(lo, hi);
+        lo = hi;
+    }
     ++rounds_;
     return done;
 }
