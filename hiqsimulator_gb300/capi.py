@@ -16,7 +16,7 @@ HEADER = os.path.join(os.path.dirname(_PKG), "include", "hqs.h")
 
 HQS_OK, HQS_ERR_RUNTIME, HQS_ERR_INVALID, HQS_ERR_CUDA, HQS_ERR_MEMORY = range(5)
 HQS_C128, HQS_C64 = 0, 1
-ARITH = {"auto": 0, "f64": 1, "df": 2, "f32": 3, "tc": 4}
+ARITH = {"auto": 0, "f64": 1, "df": 2, "f32": 3, "tc": 4, "tf32": 5, "tc64": 6}
 
 _i = ctypes.c_int
 _u64 = ctypes.c_uint64

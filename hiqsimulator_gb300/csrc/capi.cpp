@@ -110,7 +110,7 @@ int hqs_sim_create(uint64_t seed, int64_t max_local, int64_t max_cluster_size, i
         g_err = "precision must be HQS_C128 or HQS_C64";
         return HQS_ERR_INVALID;
     }
-    if (arith < HQS_ARITH_AUTO || arith > HQS_ARITH_TC) {
+    if (arith < HQS_ARITH_AUTO || arith > HQS_ARITH_TC64) {
         g_err = "unknown arithmetic";
         return HQS_ERR_INVALID;
     }
@@ -510,8 +510,7 @@ void hqs_ws_destroy(hqs_ws* ws) {
 static void check_state_args(const void* state, int n, int arith) {
     need(state != nullptr, "null state");
     need(n >= 0 && n <= 40, "n out of range");
-    need(arith == HQS_ARITH_F64 || arith == HQS_ARITH_DF || arith == HQS_ARITH_F32 || arith == HQS_ARITH_TC,
-         "unknown arithmetic");
+    need(arith >= HQS_ARITH_F64 && arith <= HQS_ARITH_TC64, "unknown arithmetic");
 }
 
 int hqs_apply_gates(hqs_ws* ws, void* state, int n, int arith, int nops, const int* k, const int* pos,

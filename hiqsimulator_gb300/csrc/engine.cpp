@@ -33,8 +33,9 @@ Engine::Engine(uint64_t seed, int64_t max_local, int64_t max_cluster_size, int p
       max_cluster_(max_cluster_size),
       rnd_eng_(seed) {
     if (arith_ == 0) arith_ = (precision_ == kC64) ? kArithF32 : kArithTC;
-    if (precision_ == kC64 && arith_ != kArithF32) fail("complex64 states use FP32 arithmetic");
-    if (precision_ == kC128 && arith_ == kArithF32) fail("complex128 states use F64, DF or TC arithmetic");
+    if (precision_ == kC64 && arith_ == kArithTC) arith_ = kArithTC64;  // tensor-core digits, two per real
+    if (precision_ == kC64 && !arith_is_c64(arith_)) fail("complex64 states use F32 or TF32 arithmetic");
+    if (precision_ == kC128 && arith_is_c64(arith_)) fail("complex128 states use F64, DF or TC arithmetic");
     capacity_ = 1024;
     cuda_check(cudaMalloc(&state_, capacity_ * elem_bytes()), "cudaMalloc(state)");
     cuda_check(cudaMemsetAsync(state_, 0, capacity_ * elem_bytes(), ws_.stream()), "cudaMemsetAsync");

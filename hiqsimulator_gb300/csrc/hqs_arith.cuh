@@ -9,6 +9,13 @@
 //        (hi, lo) pairs, and results are re-assembled into a double with
 //        integer operations. About 47-48 significant bits per operation.
 //   F32  complex64 storage, FP32 arithmetic.
+//   TC   complex128 storage; dense 3..5-qubit gates on the fp16 tensor cores
+//        as exact products of five base-2^10 digits (kernels.cu, apply_tc),
+//        every other op as DF on the raw doubles (ArithDFRaw).
+//   TC64 complex64 storage; the same tensor-core scheme with two digits,
+//        every other op as F32.
+//   TF32 complex64 storage; dense 3..5-qubit gates as 3xTF32 tensor-core
+//        products (apply_tf32), every other op as F32.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -169,6 +176,18 @@ struct ArithF32 {
     __device__ __forceinline__ static comp_t mul(const mat_t m, const comp_t v) {
         return make_float2(fmaf(m.x, v.x, -m.y * v.y), fmaf(m.x, v.y, m.y * v.x));
     }
+};
+
+// complex64 passes that also run 3xTF32 tensor-core gates: the same FP32
+// arithmetic for every other op, a separate kernel instance (register and
+// occupancy budget of the tensor-core tasks).
+struct ArithTF32 : ArithF32 {
+    static constexpr int kId = 5;
+};
+
+// complex64 passes that also run two-digit fp16 tensor-core gates.
+struct ArithTC64 : ArithF32 {
+    static constexpr int kId = 6;
 };
 
 // complex128 tiles kept as raw doubles; each operation splits its inputs into

@@ -23,11 +23,23 @@ enum Arith : int32_t {
     kArithF32 = 3,  // complex64 storage, FP32 arithmetic
     kArithTC = 4,   // complex128 storage, dense 3..5-qubit gates on the fp16 tensor cores
                     // (exact digit products, see apply_tc), the rest in double-float
+    kArithTF32 = 5, // complex64 storage, dense 3..5-qubit gates as 3xTF32 tensor-core
+                    // products (see apply_tf32), the rest in FP32
+    kArithTC64 = 6, // complex64 storage, dense 3..5-qubit gates as exact two-digit fp16
+                    // products (apply_tc), the rest in FP32
 };
+
+// complex64 (float2) states
+constexpr bool arith_is_c64(int a) { return a == kArithF32 || a == kArithTF32 || a == kArithTC64; }
+// arithmetic whose pool carries tensor-core gates
+constexpr bool arith_has_tc(int a) { return a == kArithTC || a == kArithTF32 || a == kArithTC64; }
 
 // Tensor-core digit planes: every real operand is written as kTcDigits signed
 // base-2^10 digits (|d| <= 512) scaled by a power of two shared by its row.
 constexpr int kTcDigits = 5;
+// complex64 states use two such digits per state real and three per gate real
+constexpr int kTcDigits64 = 2;
+constexpr int kTcDigits64B = 3;
 
 struct OpDesc {
     int32_t k;            // targets (0 = scalar multiply of the whole tile)
@@ -54,5 +66,12 @@ struct PassDesc {
     uint8_t ins_pos[64];  // sorted union of tile_pos and fixed-mask positions
     OpDesc ops[kMaxOpsPerPass];
 };
+
+// true when any op of the pass runs on the tensor cores
+inline bool pass_has_tc(const PassDesc& d) {
+    for (int o = 0; o < d.nops; ++o)
+        if (d.ops[o].tc) return true;
+    return false;
+}
 
 }  // namespace hqs

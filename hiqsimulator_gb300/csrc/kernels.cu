@@ -10,6 +10,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <type_traits>
 
 #include "hqs_arith.cuh"
 #include "hqs_kernels.h"
@@ -206,8 +207,10 @@ __device__ __forceinline__ uint32_t pack_digits(int d0, int d1) {
 
 // Digits of v relative to the row's largest biased exponent ebrow
 // (|v| < 2^(ebrow - 1022)), most significant first: X = round(|v| 2^(49-E_row))
-// < 2^49 is cut into five 10-bit fields, which are balanced into [-512, 511]
-// (the top one into [-512, 512]) with carries, then given v's sign.
+// < 2^49 (to nearest, ties to even: ties are frequent when few bits are
+// dropped, and rounding them away from zero would grow the state's norm) is
+// cut into five 10-bit fields, which are balanced into [-512, 511] (the top
+// one into [-512, 512]) with carries, then given v's sign.
 __device__ __forceinline__ void digits5(double v, int ebrow, int (&d)[kTcDigits]) {
     const unsigned long long u = (unsigned long long)__double_as_longlong(v);
     const uint32_t hi = (uint32_t)(u >> 32);
@@ -216,7 +219,7 @@ __device__ __forceinline__ void digits5(double v, int ebrow, int (&d)[kTcDigits]
     const int sh = 4 + ebrow - eb;  // >= 4
     if (eb != 0 && sh < 62) {
         const unsigned long long M = (u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
-        a = (M + (1ULL << (sh - 1))) >> sh;
+        a = (M + (1ULL << (sh - 1)) - 1ULL + ((M >> sh) & 1ULL)) >> sh;
     }
     const uint32_t alo = (uint32_t)a, ahi = (uint32_t)(a >> 32);
     int r4 = (int)(alo & 1023u);
@@ -242,6 +245,29 @@ __device__ __forceinline__ void digits5(double v, int ebrow, int (&d)[kTcDigits]
     d[2] = (r2 ^ sg) - sg;
     d[3] = (r3 ^ sg) - sg;
     d[4] = (r4 ^ sg) - sg;
+}
+
+// Two digits of an FP32 v relative to its row's largest biased exponent
+// ebrow (|v| < 2^(ebrow - 126)): X = round(|v| 2^(19-E_row)) <= 2^19 (to
+// nearest, ties to even) is cut into two 10-bit fields, balanced into
+// [-512, 511] (the top one into [-512, 512]) with a carry, then given v's
+// sign.
+__device__ __forceinline__ void digits2(float v, int ebrow, int (&d)[2]) {
+    const uint32_t u = __float_as_uint(v);
+    const int eb = (int)((u >> 23) & 0xFFu);
+    uint32_t a = 0;
+    const int sh = 5 + ebrow - eb;  // >= 5
+    if (eb != 0 && sh < 32) {
+        const uint32_t M = (u & 0x7FFFFFu) | 0x800000u;
+        a = (M + (1u << (sh - 1)) - 1u + ((M >> sh) & 1u)) >> sh;
+    }
+    int r1 = (int)(a & 1023u), r0 = (int)(a >> 10);
+    const int c = (r1 + 512) >> 10;
+    r1 -= c << 10;
+    r0 += c;
+    const int sg = (int)(u >> 31) ? -1 : 0;
+    d[0] = (r0 ^ sg) - sg;
+    d[1] = (r1 ^ sg) - sg;
 }
 
 // S * 2^sc as the nearest double (ties away from zero), built from bits.
@@ -291,12 +317,39 @@ __host__ __device__ constexpr int tc_acc(int i, int j) {
 }
 __host__ __device__ constexpr int tc_level(int a) { return a == 0 ? 0 : a <= 2 ? 1 : a <= 5 ? 2 : a == 6 ? 3 : 4; }
 
-// Pool layout of a tensor-core gate (bytes): int32 E_col[2D], then kTcDigits
+// Digit counts of each amplitude type (state digits A, gate digits B) and
+// the products kept. complex128: five and five, levels 0..4 (above). complex64:
+// two state digits, three gate digits, products (0,0), (0,1), (1,0), (0,2) in
+// four accumulators: the gate is exact to 2^-29 of its column scale against
+// the state's top digit, and the dropped products (below 2^-19 of the
+// row scale) depend on the state's low digit, so they add noise but no
+// systematic change of the norm. All digits round to nearest.
+template <class V>
+struct TcDigits;
+template <>
+struct TcDigits<double2> {
+    static constexpr int kA = kTcDigits, kB = kTcDigits, kAcc = 8;
+    __device__ static constexpr bool keep(int i, int j) { return i + j < kTcDigits; }
+    __device__ static constexpr int acc(int i, int j) { return tc_acc(i, j); }
+};
+template <>
+struct TcDigits<float2> {
+    static constexpr int kA = kTcDigits64, kB = kTcDigits64B, kAcc = 4;
+    __device__ static constexpr bool keep(int i, int j) { return i + j <= 1 || (i == 0 && j == 2); }
+    __device__ static constexpr int acc(int i, int j) { return i + j == 0 ? 0 : i + j == 1 ? 1 + i : 3; }
+};
+
+// Pool layout of a tensor-core gate (bytes): int32 E_col[2D], then NDB digit
 // planes of B^T, each 2D rows of (2D + 8) fp16 (row j holds column j of B).
-template <int K>
-__device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double2* __restrict__ dst,
+template <int K, class V>
+__device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restrict__ dst,
                                          const unsigned char* __restrict__ pool, const OpDesc& op, int q,
                                          unsigned char* __restrict__ scratch) {
+    using TD = TcDigits<V>;
+    constexpr bool kC128 = std::is_same<V, double2>::value;
+    constexpr int ND = TD::kA;
+    constexpr int NDB = TD::kB;
+    constexpr int NACC = TD::kAcc;
     constexpr int D = 1 << K;
     constexpr int KK = 2 * D;
     constexpr int RH = KK + 8;  // fp16 per plane row (padded against bank conflicts)
@@ -304,7 +357,7 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
     const int* ecol = reinterpret_cast<const int*>(pool);
     const __half* planeB = reinterpret_cast<const __half*>(pool + 4 * KK);
     __half* planeA = reinterpret_cast<__half*>(scratch);
-    int* erow = reinterpret_cast<int*>(scratch + (size_t)kTcDigits * G * RH * 2);
+    int* erow = reinterpret_cast<int*>(scratch + (size_t)ND * G * RH * 2);
 
     int ss[K];
     uint32_t bitv[K];
@@ -348,9 +401,14 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
         int eb = 0;
 #pragma unroll
         for (int u = 0; u < CPI; ++u) {
-            const double2 x = src[Lb + offset_of(ch * CPI + u)];
-            eb = max(eb, (int)(((unsigned long long)__double_as_longlong(x.x) >> 52) & 0x7FFu));
-            eb = max(eb, (int)(((unsigned long long)__double_as_longlong(x.y) >> 52) & 0x7FFu));
+            const V x = src[Lb + offset_of(ch * CPI + u)];
+            if constexpr (kC128) {
+                eb = max(eb, (int)(((unsigned long long)__double_as_longlong(x.x) >> 52) & 0x7FFu));
+                eb = max(eb, (int)(((unsigned long long)__double_as_longlong(x.y) >> 52) & 0x7FFu));
+            } else {
+                eb = max(eb, (int)((__float_as_uint(x.x) >> 23) & 0xFFu));
+                eb = max(eb, (int)((__float_as_uint(x.y) >> 23) & 0xFFu));
+            }
         }
         if (eb) atomicMax(&erow[g], eb);
     }
@@ -359,18 +417,23 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
         const int g = it % G, ch = it / G;
         const uint32_t Lb = group_base(g);
         const int ebrow = erow[g];
-        uint32_t w[kTcDigits][CPI];
+        uint32_t w[ND][CPI];
 #pragma unroll
         for (int u = 0; u < CPI; ++u) {
-            const double2 x = src[Lb + offset_of(ch * CPI + u)];
-            int dr[kTcDigits], di[kTcDigits];
-            digits5(x.x, ebrow, dr);
-            digits5(x.y, ebrow, di);
+            const V x = src[Lb + offset_of(ch * CPI + u)];
+            int dr[ND], di[ND];
+            if constexpr (kC128) {
+                digits5(x.x, ebrow, dr);
+                digits5(x.y, ebrow, di);
+            } else {
+                digits2(x.x, ebrow, dr);
+                digits2(x.y, ebrow, di);
+            }
 #pragma unroll
-            for (int sdx = 0; sdx < kTcDigits; ++sdx) w[sdx][u] = pack_digits(dr[sdx], di[sdx]);
+            for (int sdx = 0; sdx < ND; ++sdx) w[sdx][u] = pack_digits(dr[sdx], di[sdx]);
         }
 #pragma unroll
-        for (int sdx = 0; sdx < kTcDigits; ++sdx)
+        for (int sdx = 0; sdx < ND; ++sdx)
             *reinterpret_cast<uint2*>(planeA + (size_t)sdx * G * RH + (size_t)g * RH + ch * 2 * CPI) =
                 make_uint2(w[sdx][0], w[sdx][1]);
     }
@@ -382,9 +445,9 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
     constexpr int NT = KK / 8;
     for (int task = warp; task < mtiles * NT; task += nwarps) {
         const int mt = task / NT, nt = task % NT;
-        float acc[8][4];
+        float acc[NACC][4];
 #pragma unroll
-        for (int a = 0; a < 8; ++a)
+        for (int a = 0; a < NACC; ++a)
 #pragma unroll
             for (int e = 0; e < 4; ++e) acc[a][e] = 0.f;
         const int arow = mt * 16 + (lane & 7) + ((lane >> 3) & 1) * 8;
@@ -393,22 +456,23 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
         for (int kp = 0; kp < KK / 32 + (KK < 32 ? 1 : 0); ++kp) {
             // two k16 steps per iteration (one when KK == 16): B fragments for
             // both come from one ldmatrix.x4
-            uint32_t af[kTcDigits][4];
+            uint32_t af[ND][4];
             const int ks0 = kp * 2;
 #pragma unroll
             for (int half = 0; half < (KK < 32 ? 1 : 2); ++half) {
                 const int ks = ks0 + half;
                 const int acol = ks * 16 + (lane >> 4) * 8;
 #pragma unroll
-                for (int s = 0; s < kTcDigits; ++s)
+                for (int s = 0; s < ND; ++s)
                     ldsm_x4(af[s], planeA + (size_t)s * G * RH + (size_t)arow * RH + acol);
                 const int bcol = ks * 16 + ((lane >> 3) & 1) * 8;
 #pragma unroll
-                for (int j = 0; j < kTcDigits; ++j) {
+                for (int j = 0; j < NDB; ++j) {
                     uint32_t bf[2];
                     ldsm_x2(bf, planeB + (size_t)j * KK * RH + (size_t)brow * RH + bcol);
 #pragma unroll
-                    for (int i = 0; i + j < kTcDigits; ++i) mma_f16(acc[tc_acc(i, j)], af[i], bf[0], bf[1]);
+                    for (int i = 0; i < ND; ++i)
+                        if (TD::keep(i, j)) mma_f16(acc[TD::acc(i, j)], af[i], bf[0], bf[1]);
                 }
             }
         }
@@ -426,24 +490,150 @@ __device__ __forceinline__ void apply_tc(const double2* __restrict__ src, double
                 dst[idx] = src[idx];
                 continue;
             }
-            const int er = erow[g] - 1022;
-            double outv[2];
+            if constexpr (kC128) {
+                const int er = erow[g] - 1022;
+                double outv[2];
 #pragma unroll
-            for (int c2 = 0; c2 < 2; ++c2) {
-                // accumulators hold integers: level sums as one fixed-point
-                // int64 S = L0 2^30 + L1 2^20 + L2 2^10 + L3 + L4 2^-10 (< 2^55),
-                // value = S * 2^(E_row + E_col - 48)
-                const int e = h * 2 + c2;
-                const long long L0 = __float2int_rn(acc[0][e]);
-                const long long L1 = (long long)__float2int_rn(acc[1][e]) + __float2int_rn(acc[2][e]);
-                const long long L2 =
-                    (long long)__float2int_rn(acc[3][e]) + __float2int_rn(acc[4][e]) + __float2int_rn(acc[5][e]);
-                const long long L3 = __float2int_rn(acc[6][e]);
-                const long long L4 = __float2int_rn(acc[7][e]);
-                const long long S = (L0 << 30) + (L1 << 20) + (L2 << 10) + L3 + (L4 >> 10);
-                outv[c2] = fixed_to_double(S, er + ecol[nt * 8 + tig * 2 + c2] - 48);
+                for (int c2 = 0; c2 < 2; ++c2) {
+                    // accumulators hold integers: level sums as one fixed-point
+                    // int64 S = L0 2^30 + L1 2^20 + L2 2^10 + L3 + L4 2^-10 (< 2^55),
+                    // value = S * 2^(E_row + E_col - 48)
+                    const int e = h * 2 + c2;
+                    const long long L0 = __float2int_rn(acc[0][e]);
+                    const long long L1 = (long long)__float2int_rn(acc[1][e]) + __float2int_rn(acc[2][e]);
+                    const long long L2 = (long long)__float2int_rn(acc[3][e]) + __float2int_rn(acc[4][e]) +
+                                         __float2int_rn(acc[5][e]);
+                    const long long L3 = __float2int_rn(acc[6][e]);
+                    const long long L4 = __float2int_rn(acc[7][e]);
+                    const long long S = (L0 << 30) + (L1 << 20) + (L2 << 10) + L3 + (L4 >> 10);
+                    outv[c2] = fixed_to_double(S, er + ecol[nt * 8 + tig * 2 + c2] - 48);
+                }
+                dst[idx] = make_double2(outv[0], outv[1]);
+            } else {
+                const int er = erow[g] - 126;
+                float outv[2];
+#pragma unroll
+                for (int c2 = 0; c2 < 2; ++c2) {
+                    // S = L0 2^20 + L1 2^10 + L2 (< 2^45),
+                    // value = S * 2^(E_row + E_col - 38)
+                    const int e = h * 2 + c2;
+                    const long long L0 = __float2int_rn(acc[0][e]);
+                    const long long L1 = (long long)__float2int_rn(acc[1][e]) + __float2int_rn(acc[2][e]);
+                    const long long L2 = __float2int_rn(acc[3][e]);
+                    const long long S = (L0 << 20) + (L1 << 10) + L2;
+                    outv[c2] = ldexpf(__ll2float_rn(S), er + ecol[nt * 8 + tig * 2 + c2] - 38);
+                }
+                dst[idx] = make_float2(outv[0], outv[1]);
             }
-            dst[idx] = make_double2(outv[0], outv[1]);
+        }
+    }
+}
+
+// ------------------------------------------------- complex64 3xTF32 gates
+//
+// A dense k-qubit gate (k = 3..5) on complex64 amplitudes in the same real
+// form as apply_tc: a tile's G = 2^(q-k) index groups are the rows of X
+// (G x 2D reals, interleaved re/im of the group's D inputs), Y = X B. Each
+// FP32 operand x is split into two TF32 parts, hi = rna(x) and
+// lo = rna(x - hi) (x - hi is exact in FP32), and Y accumulates
+// lo*hi + hi*lo + hi*hi with m16n8k8 TF32 MMAs in FP32; the dropped lo*lo
+// term is below 2^-21 of each product. A fragments are read straight from
+// the tile buffer; B comes split and in fragment order from the pass pool:
+// for k-step ks and n-tile nt, lane l holds float4 {hi b0, hi b1, lo b0,
+// lo b1} with b0 = B[8ks + l%4][8nt + l/4], b1 = B[8ks + l%4 + 4][8nt + l/4].
+
+__device__ __forceinline__ uint32_t tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(float (&c)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+template <int K>
+__device__ __forceinline__ void apply_tf32(const float2* __restrict__ src, float2* __restrict__ dst,
+                                           const float4* __restrict__ frag, const OpDesc& op, int q) {
+    constexpr int D = 1 << K;
+    constexpr int KK = 2 * D;
+    constexpr int NT = KK / 8;              // n-tiles (8 output reals) and k-steps (8 input reals)
+    constexpr int NTW = NT < 4 ? NT : 4;    // n-tiles per warp task
+    constexpr int NCH = NT / NTW;
+    const int G = 1 << (q - K);
+    const int MT = G >> 4;
+
+    int ss[K];
+    uint32_t bitv[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        ss[j] = op.tslot[j];
+        bitv[j] = 1u << op.tslot[j];
+    }
+#pragma unroll
+    for (int a = 1; a < K; ++a)
+#pragma unroll
+        for (int b = K - 1; b >= a; --b)
+            if (ss[b - 1] > ss[b]) { const int t = ss[b]; ss[b] = ss[b - 1]; ss[b - 1] = t; }
+    auto group_base = [&](uint32_t g) {
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            const uint32_t low = g & ((1u << ss[j]) - 1u);
+            g = ((g - low) << 1) | low;
+        }
+        return g;
+    };
+    auto offset_of = [&](int c) {
+        uint32_t o = 0;
+#pragma unroll
+        for (int j = 0; j < K; ++j)
+            if ((c >> j) & 1) o |= bitv[j];
+        return o;
+    };
+
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int gid = lane >> 2, tig = lane & 3;
+    for (int task = warp; task < MT * NCH; task += nwarps) {
+        const int mt = task / NCH, nc = task % NCH;
+        const uint32_t Lb0 = group_base(mt * 16 + gid), Lb1 = group_base(mt * 16 + gid + 8);
+        float acc[NTW][4];
+#pragma unroll
+        for (int j = 0; j < NTW; ++j)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) acc[j][e] = 0.f;
+#pragma unroll
+        for (int ks = 0; ks < NT; ++ks) {
+            // columns tig and tig + 4 of this k-step: part tig & 1 of inputs
+            // 4 ks + tig / 2 and 4 ks + 2 + tig / 2
+            const uint32_t o0 = offset_of(ks * 4 + (tig >> 1)), o1 = offset_of(ks * 4 + 2 + (tig >> 1));
+            const float2 x00 = src[Lb0 + o0], x10 = src[Lb1 + o0], x01 = src[Lb0 + o1], x11 = src[Lb1 + o1];
+            const bool im = (tig & 1) != 0;
+            const float av[4] = {im ? x00.y : x00.x, im ? x10.y : x10.x, im ? x01.y : x01.x, im ? x11.y : x11.x};
+            uint32_t ah[4], al[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                ah[e] = tf32_rna(av[e]);
+                al[e] = tf32_rna(av[e] - __uint_as_float(ah[e]));
+            }
+#pragma unroll
+            for (int j = 0; j < NTW; ++j) {
+                const float4 b = frag[(ks * NT + nc * NTW + j) * 32 + lane];
+                mma_tf32(acc[j], al, __float_as_uint(b.x), __float_as_uint(b.y));
+                mma_tf32(acc[j], ah, __float_as_uint(b.z), __float_as_uint(b.w));
+                mma_tf32(acc[j], ah, __float_as_uint(b.x), __float_as_uint(b.y));
+            }
+        }
+        // columns 2 tig, 2 tig + 1 of n-tile nt: output nt * 4 + tig
+        const bool ok0 = (Lb0 & op.ctrl_local) == op.ctrl_local;
+        const bool ok1 = (Lb1 & op.ctrl_local) == op.ctrl_local;
+#pragma unroll
+        for (int j = 0; j < NTW; ++j) {
+            const uint32_t orow = offset_of((nc * NTW + j) * 4 + tig);
+            dst[Lb0 + orow] = ok0 ? make_float2(acc[j][0], acc[j][1]) : src[Lb0 + orow];
+            dst[Lb1 + orow] = ok1 ? make_float2(acc[j][2], acc[j][3]) : src[Lb1 + orow];
         }
     }
 }
@@ -514,13 +704,28 @@ __device__ __forceinline__ void pass_tile(typename A::store_t* __restrict__ stat
             __syncthreads();
             continue;
         }
-        if constexpr (A::kId == 4) {
+        if constexpr (A::kId == 5) {
+            if (op.tc) {
+                const float4* frag = reinterpret_cast<const float4*>(sm.smat + op.mat_off);
+                switch (op.k) {
+                    case 3: apply_tf32<3>(src, dst, frag, op, d.q); break;
+                    case 4: apply_tf32<4>(src, dst, frag, op, d.q); break;
+                    default: apply_tf32<5>(src, dst, frag, op, d.q); break;
+                }
+                __syncthreads();
+                C* tmp = src;
+                src = dst;
+                dst = tmp;
+                continue;
+            }
+        }
+        if constexpr (A::kId == 4 || A::kId == 6) {
             if (op.tc) {
                 const unsigned char* pool = reinterpret_cast<const unsigned char*>(sm.smat + op.mat_off);
                 switch (op.k) {
-                    case 3: apply_tc<3>(src, dst, pool, op, d.q, sm.tcs); break;
-                    case 4: apply_tc<4>(src, dst, pool, op, d.q, sm.tcs); break;
-                    default: apply_tc<5>(src, dst, pool, op, d.q, sm.tcs); break;
+                    case 3: apply_tc<3, C>(src, dst, pool, op, d.q, sm.tcs); break;
+                    case 4: apply_tc<4, C>(src, dst, pool, op, d.q, sm.tcs); break;
+                    default: apply_tc<5, C>(src, dst, pool, op, d.q, sm.tcs); break;
                 }
                 __syncthreads();
                 C* tmp = src;
@@ -546,8 +751,12 @@ __device__ __forceinline__ void pass_tile(typename A::store_t* __restrict__ stat
     __syncthreads();
 }
 
+// resident CTAs per SM the pass kernels are compiled for (register cap):
+// digit-plane tensor-core passes 3, 3xTF32 passes 2, the rest 4
+__host__ __device__ constexpr int pass_min_blocks(int id) { return (id == 4 || id == 6) ? 3 : id == 5 ? 2 : 4; }
+
 template <class A>
-__global__ void __launch_bounds__(kThreads, A::kId == 4 ? 3 : 4) pass_kernel(typename A::store_t* __restrict__ state,
+__global__ void __launch_bounds__(kThreads, pass_min_blocks(A::kId)) pass_kernel(typename A::store_t* __restrict__ state,
                                                                              const typename A::mat_t* __restrict__ mats,
                                                                              const __grid_constant__ PassDesc d) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -561,7 +770,7 @@ __global__ void __launch_bounds__(kThreads, A::kId == 4 ? 3 : 4) pass_kernel(typ
 // belongs to the item whose tile range contains it; each CTA walks its tiles
 // in increasing T and re-stages the pass when it crosses into a new item.
 template <class A>
-__global__ void __launch_bounds__(kThreads, A::kId == 4 ? 3 : 4) batch_pass_kernel(const BatchItem* __restrict__ items,
+__global__ void __launch_bounds__(kThreads, pass_min_blocks(A::kId)) batch_pass_kernel(const BatchItem* __restrict__ items,
                                                                                    int nitems, uint64_t total_tiles) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ PassDesc sd;
@@ -925,15 +1134,18 @@ int device_sm_count() {
     return sms;
 }
 
-// Kernels other than the fused pass treat tensor-core mode as double-float.
-static inline int base_arith(int a) { return a == kArithTC ? kArithDF : a; }
+// Kernels other than the fused pass treat tensor-core modes as their base
+// arithmetic: double-float for complex128, FP32 for complex64.
+static inline int base_arith(int a) {
+    return a == kArithTC ? kArithDF : (a == kArithTF32 || a == kArithTC64) ? kArithF32 : a;
+}
 
 size_t pass_smem_bytes(int arith, const PassDesc& d) {
     switch (arith) {
         case kArithF64: return pass_smem_t<ArithF64>(d);
         case kArithDF: return pass_smem_t<ArithDF>(d);
-        case kArithTC: return d.tc_bytes ? pass_smem_t<ArithDFRaw>(d) : pass_smem_t<ArithDF>(d);
-        default: return pass_smem_t<ArithF32>(d);
+        case kArithTC: return pass_has_tc(d) ? pass_smem_t<ArithDFRaw>(d) : pass_smem_t<ArithDF>(d);
+        default: return pass_smem_t<ArithF32>(d);  // F32, TF32, TC64: same tile and pool element
     }
 }
 
@@ -944,8 +1156,12 @@ cudaError_t launch_pass(int arith, void* state, const void* mats, const PassDesc
         case kArithF32: return launch_pass_t<ArithF32>(state, mats, d, s);
         // passes without tensor-core gates run the double-float kernel (same
         // matrix format, fewer registers, more resident CTAs)
-        case kArithTC: return d.tc_bytes ? launch_pass_t<ArithDFRaw>(state, mats, d, s)
-                                         : launch_pass_t<ArithDF>(state, mats, d, s);
+        case kArithTC: return pass_has_tc(d) ? launch_pass_t<ArithDFRaw>(state, mats, d, s)
+                                             : launch_pass_t<ArithDF>(state, mats, d, s);
+        case kArithTF32: return pass_has_tc(d) ? launch_pass_t<ArithTF32>(state, mats, d, s)
+                                               : launch_pass_t<ArithF32>(state, mats, d, s);
+        case kArithTC64: return pass_has_tc(d) ? launch_pass_t<ArithTC64>(state, mats, d, s)
+                                               : launch_pass_t<ArithF32>(state, mats, d, s);
         default: return cudaErrorInvalidValue;
     }
 }
@@ -958,6 +1174,10 @@ cudaError_t launch_batch(int arith, bool tc, const BatchItem* d_items, int nitem
         case kArithF32: return launch_batch_t<ArithF32>(d_items, nitems, total_tiles, smem, s);
         case kArithTC: return tc ? launch_batch_t<ArithDFRaw>(d_items, nitems, total_tiles, smem, s)
                                  : launch_batch_t<ArithDF>(d_items, nitems, total_tiles, smem, s);
+        case kArithTF32: return tc ? launch_batch_t<ArithTF32>(d_items, nitems, total_tiles, smem, s)
+                                   : launch_batch_t<ArithF32>(d_items, nitems, total_tiles, smem, s);
+        case kArithTC64: return tc ? launch_batch_t<ArithTC64>(d_items, nitems, total_tiles, smem, s)
+                                   : launch_batch_t<ArithF32>(d_items, nitems, total_tiles, smem, s);
         default: return cudaErrorInvalidValue;
     }
 }

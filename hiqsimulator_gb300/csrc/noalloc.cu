@@ -109,7 +109,7 @@ extern "C" int hqs_probability_noalloc(const void* state, int n, int arith, uint
                                        double* d_out, void* stream) {
     if (!state || !d_out) return fail(HQS_ERR_INVALID, "hqs_probability_noalloc: null state or output pointer");
     if (n < 0 || n > 40) return fail(HQS_ERR_INVALID, "hqs_probability_noalloc: n out of range");
-    if (arith != HQS_ARITH_F64 && arith != HQS_ARITH_DF && arith != HQS_ARITH_F32 && arith != HQS_ARITH_TC)
+    if (arith < HQS_ARITH_F64 || arith > HQS_ARITH_TC64)
         return fail(HQS_ERR_INVALID, "hqs_probability_noalloc: unknown arithmetic");
     if (n < 64 && (mask >> n) != 0) return fail(HQS_ERR_INVALID, "hqs_probability_noalloc: mask out of range");
     NoAllocMask m;

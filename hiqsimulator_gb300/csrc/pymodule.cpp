@@ -47,7 +47,9 @@ int parse_arith(const std::string& a) {
     if (a == "df") return HQS_ARITH_DF;
     if (a == "f32") return HQS_ARITH_F32;
     if (a == "tc") return HQS_ARITH_TC;
-    throw py::value_error("arith must be 'auto', 'f64', 'df', 'tc' or 'f32'");
+    if (a == "tf32") return HQS_ARITH_TF32;
+    if (a == "tc64") return HQS_ARITH_TC64;
+    throw py::value_error("arith must be 'auto', 'f64', 'df', 'tc', 'f32' or 'tf32'");
 }
 
 std::string env_or(const char* name, const char* dflt) {
@@ -232,7 +234,8 @@ public:
     std::string arith() const {
         int p = 0, a = 0;
         check(hqs_sim_info(h_, &p, &a));
-        return a == HQS_ARITH_F64 ? "f64" : a == HQS_ARITH_DF ? "df" : a == HQS_ARITH_TC ? "tc" : "f32";
+        return a == HQS_ARITH_F64 ? "f64" : a == HQS_ARITH_DF ? "df" : a == HQS_ARITH_TC ? "tc"
+               : a == HQS_ARITH_TF32 ? "tf32" : a == HQS_ARITH_TC64 ? "tc" : "f32";
     }
     void enable_pass_timing(bool on) { check(hqs_sim_set_pass_timing(h_, on ? 1 : 0)); }
     py::dict pass_timing() {

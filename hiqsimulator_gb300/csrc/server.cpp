@@ -43,7 +43,8 @@ Server::Server(int precision, int arith, uint64_t budget_bytes, int max_active, 
       cluster_(std::max(1, std::min(cluster_size, kMaxK))),
       budget_(budget_bytes) {
     if (arith_ == 0) arith_ = precision_ == 1 ? kArithF32 : kArithTC;
-    if ((precision_ == 1) != (arith_ == kArithF32)) throw std::invalid_argument("server: precision/arith mismatch");
+    if (precision_ == 1 && arith_ == kArithTC) arith_ = kArithTC64;
+    if ((precision_ == 1) != arith_is_c64(arith_)) throw std::invalid_argument("server: precision/arith mismatch");
     for (int i = 0; i < 2; ++i) cuda_check(cudaEventCreateWithFlags(&staging_done_[i], cudaEventDisableTiming), "cudaEventCreate");
     cuda_check(cudaMalloc(&blocks_dev_, sizeof(double) << 15), "cudaMalloc(blocks)");
     cuda_check(cudaMallocHost(&blocks_host_, sizeof(double) << 15), "cudaMallocHost(blocks)");
@@ -131,9 +132,9 @@ uint64_t Server::submit(int n, const std::vector<ServerGate>& gates, int kind, d
     }
     flush();
     // digit planes of tensor-core-sized gates once, not every round
-    if (arith_ == kArithTC)
+    if (arith_has_tc(arith_))
         for (auto& op : r.ops)
-            if (op.k >= 3 && !op.diag) op.tc_pool = make_tc_pool(op);
+            if (op.k >= 3 && !op.diag) op.tc_pool = make_tc_pool(arith_, op);
     queue_.push_back(std::move(r));
     return queue_.back().id;
 }
@@ -259,8 +260,8 @@ std::vector<ServerResult> Server::step() {
         const size_t window = std::min<size_t>(r.ops.size() - r.next, kMaxOpsPerPass);
         std::vector<size_t> first;
         std::vector<PassPlan> plans = plan_passes(r.n, arith_, r.ops.data() + r.next, window, 10, 16, &first, 1);
-        Planned p{&r, plans[0], r.next, plans[0].desc.tc_bytes != 0, 0};
-        p.smem = pass_smem_bytes(p.tc ? kArithTC : (arith_ == kArithTC ? kArithDF : arith_), p.plan.desc);
+        Planned p{&r, plans[0], r.next, pass_has_tc(plans[0].desc), 0};
+        p.smem = pass_smem_bytes(arith_, p.plan.desc);
         r.next += (size_t)plans[0].desc.nops;
         ++r.passes;
         planned.push_back(p);

@@ -91,27 +91,43 @@ void Workspace::ensure_pinned(size_t bytes) {
 
 static int popc64(uint64_t v) { return __builtin_popcountll(v); }
 
-// Pool bytes of a tensor-core gate: int32 E_col[2D] + kTcDigits planes of
-// 2D rows x (2D + 8) fp16.
-static size_t tc_pool_bytes(int k) {
+// Digits per state real (A) and per gate real (B) of the digit-plane
+// tensor-core modes.
+static int tc_digits(int arith) { return arith == kArithTC64 ? kTcDigits64 : kTcDigits; }
+static int tc_digits_b(int arith) { return arith == kArithTC64 ? kTcDigits64B : kTcDigits; }
+
+// Pool bytes of a tensor-core gate. Digit planes: int32 E_col[2D] + one
+// plane per digit of 2D rows x (2D + 8) fp16. 3xTF32: (2D/8)^2 fragment
+// blocks of 32 lanes x float4.
+static size_t tc_pool_bytes(int arith, int k) {
     const size_t KK = (size_t)2 << k;
-    return 4 * KK + (size_t)kTcDigits * KK * (KK + 8) * 2;
+    if (arith == kArithTF32) return KK * KK * 8;
+    return 4 * KK + (size_t)tc_digits_b(arith) * KK * (KK + 8) * 2;
 }
 
-static bool tc_candidate(int arith, const GateOp& op) { return arith == kArithTC && !op.diag && op.k >= 3; }
+// Shared-memory scratch of a digit-plane gate on a 2^q tile: the tile's
+// digit planes (G = 2^(q-k) rows) and the rows' exponents.
+static size_t tc_scratch_bytes(int arith, int q, int k) {
+    if (arith == kArithTF32) return 0;
+    const size_t G = (size_t)1 << (q - k), KK = (size_t)2 << k;
+    return (size_t)tc_digits(arith) * G * (KK + 8) * 2 + 4 * G;
+}
+
+static bool tc_candidate(int arith, const GateOp& op) { return arith_has_tc(arith) && !op.diag && op.k >= 3; }
 
 // Pool elements (of mat_elem_bytes) an op occupies.
 static size_t pool_elems(int arith, const GateOp& op, bool tc) {
     const size_t melem = Workspace::mat_elem_bytes(arith);
-    if (tc) return (tc_pool_bytes(op.k) + melem - 1) / melem;
+    if (tc) return (tc_pool_bytes(arith, op.k) + melem - 1) / melem;
     return op.m.size();
 }
 
 std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t nops, int max_tile_bits, int max_ops,
                                   std::vector<size_t>* op_first, size_t max_passes) {
     const size_t melem = Workspace::mat_elem_bytes(arith);
-    const size_t store = (arith == kArithF32) ? 8 : 16;
-    const size_t mat_budget = 64 * 1024;
+    const size_t store = arith_is_c64(arith) ? 8 : 16;
+    // staged matrices per pass; 3xTF32 passes take two 5-qubit gates
+    const size_t mat_budget = (arith == kArithTF32 ? 72 : 64) * 1024;
     max_tile_bits = std::max(5, std::min(max_tile_bits, kMaxTileBits));
     max_ops = std::max(1, std::min(max_ops, kMaxOpsPerPass));
     std::vector<PassPlan> plans;
@@ -136,11 +152,13 @@ std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t no
         std::memset(&d, 0, sizeof(d));
         // tile: the pass's targets plus at least 4 low positions, 2^10 amplitudes
         // at least (enough index groups for every thread), at most 2^max_tile_bits
-        // tensor-core passes use 2^9-amplitude tiles (16 index groups for a 5-qubit
-        // gate) so that three CTAs fit on an SM next to the gate's digit planes
+        // complex128 digit-plane passes use 2^9-amplitude tiles (16 index
+        // groups for a 5-qubit gate) so that three CTAs fit on an SM next to
+        // the gate's digit planes; 3xTF32 passes 2^11 (64 groups: every warp
+        // gets a task of four n-tiles)
         bool has_tc = false;
         for (size_t o = i; o < j; ++o) has_tc = has_tc || tc_candidate(arith, ops[o]);
-        const int base_q = has_tc ? 9 : 10;
+        const int base_q = !has_tc ? 10 : arith == kArithTF32 ? 11 : arith == kArithTC ? 9 : 10;
         int q = std::min(n, std::max(popc64(tset), std::min(max_tile_bits, std::max(popc64(tset) + 4, base_q))));
         // keep the pass within one CTA's shared memory: shrink the tile (not
         // below the targets), then give up tensor-core gates if still too big
@@ -149,11 +167,8 @@ std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t no
             size_t mat = 0, tcb = 0;
             for (size_t o = i; o < j; ++o) {
                 const bool tc = tcok && tc_candidate(arith, ops[o]) && qq >= ops[o].k + 4;
-                mat += pool_elems(arith, ops[o], tc) * melem;
-                if (tc) {
-                    const size_t G = (size_t)1 << (qq - ops[o].k), KK = (size_t)2 << ops[o].k;
-                    tcb = std::max(tcb, (size_t)kTcDigits * G * (KK + 8) * 2 + 4 * G);
-                }
+                mat += pool_elems(arith, ops[o], tc) * melem + (tc ? 8 : 0);
+                if (tc) tcb = std::max(tcb, tc_scratch_bytes(arith, qq, ops[o].k));
             }
             return mat + 2 * (store << qq) + 8 * ((size_t)1 << qq) + 32 + tcb;
         };
@@ -191,10 +206,9 @@ std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t no
             od.diag = op.diag ? 1 : 0;
             // tensor-core gates need at least 16 index groups per tile
             od.tc = (allow_tc && tc_candidate(arith, op) && q >= op.k + 4) ? 1 : 0;
-            if (od.tc) {
-                const size_t G = (size_t)1 << (q - op.k), KK = (size_t)2 << op.k;
-                tcb = std::max(tcb, (size_t)kTcDigits * G * (KK + 8) * 2 + 4 * G);
-            }
+            // 3xTF32 fragments are read as float4: 16-byte aligned in the pool
+            if (od.tc && arith == kArithTF32) moff = (moff + 1) & ~1u;
+            if (od.tc) tcb = std::max(tcb, tc_scratch_bytes(arith, q, op.k));
             od.ctrl_outer = op.ctrl_mask & ~tile;
             uint32_t cl = 0;
             for (int b = 0; b < n; ++b)
@@ -229,35 +243,35 @@ static int biased_exponent(double v) {
     return (int)((u >> 52) & 0x7FF);
 }
 
-// The five balanced base-2^10 digits of v relative to the biased exponent
+// The nd balanced base-2^10 digits of v relative to the biased exponent
 // ebmax of its column (same rule as the device-side digits of the state):
-// a = round(|v| 2^(49 - E)) cut into 10-bit fields, balanced into [-512, 511]
-// with carries upward, then given v's sign.
-static void digits_host(double v, int ebmax, int* d) {
+// a = round(|v| 2^(10 nd - 1 - E)) (to nearest, ties to even) cut into 10-bit
+// fields, balanced into [-512, 511] with carries upward, then given v's sign.
+static void digits_host(double v, int ebmax, int nd, int* d) {
     uint64_t u;
     std::memcpy(&u, &v, 8);
     const int eb = (int)((u >> 52) & 0x7FF);
     uint64_t a = 0;
-    const int sh = 4 + ebmax - eb;
+    const int sh = 4 + 10 * (kTcDigits - nd) + ebmax - eb;
     if (eb != 0 && sh < 62) {
         const uint64_t M = (u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
-        a = (M + (1ULL << (sh - 1))) >> sh;
+        a = (M + (1ULL << (sh - 1)) - 1ULL + ((M >> sh) & 1ULL)) >> sh;
     }
     int r[kTcDigits];
-    for (int i = 0; i < kTcDigits; ++i) r[kTcDigits - 1 - i] = (int)((a >> (10 * i)) & 1023u);
-    r[0] = (int)(a >> 40);
-    for (int i = kTcDigits - 1; i >= 1; --i) {
+    for (int i = 0; i < nd; ++i) r[nd - 1 - i] = (int)((a >> (10 * i)) & 1023u);
+    r[0] = (int)(a >> (10 * (nd - 1)));
+    for (int i = nd - 1; i >= 1; --i) {
         const int c = (r[i] + 512) >> 10;
         r[i] -= c << 10;
         r[i - 1] += c;
     }
     const bool neg = (u >> 63) != 0;
-    for (int i = 0; i < kTcDigits; ++i) d[i] = neg ? -r[i] : r[i];
+    for (int i = 0; i < nd; ++i) d[i] = neg ? -r[i] : r[i];
 }
 
 // Real form of a complex gate for the tensor-core path (B with Y = X B, X the
 // interleaved real and imaginary parts of a group's inputs).
-static void convert_tc(const GateOp& op, unsigned char* dst) {
+static void convert_tc(const GateOp& op, int nd, unsigned char* dst) {
     const int D = 1 << op.k, KK = 2 * D, RH = KK + 8;
     // interleaved real form: row 2c + p_in is part p_in of input c, column
     // 2r + p_out part p_out of output r
@@ -269,17 +283,60 @@ static void convert_tc(const GateOp& op, unsigned char* dst) {
     };
     int32_t* ecol = reinterpret_cast<int32_t*>(dst);
     uint16_t* planes = reinterpret_cast<uint16_t*>(dst + 4 * KK);
-    std::memset(planes, 0, (size_t)kTcDigits * KK * RH * 2);
+    std::memset(planes, 0, (size_t)nd * KK * RH * 2);
     for (int j = 0; j < KK; ++j) {
         int ebmax = 0;
         for (int kk = 0; kk < KK; ++kk) ebmax = std::max(ebmax, biased_exponent(bval(kk, j)));
         ecol[j] = ebmax - 1022;
         for (int kk = 0; kk < KK; ++kk) {
             int d[kTcDigits];
-            digits_host(bval(kk, j), ebmax, d);
-            for (int s2 = 0; s2 < kTcDigits; ++s2) planes[(size_t)s2 * KK * RH + (size_t)j * RH + kk] = half_of_int(d[s2]);
+            digits_host(bval(kk, j), ebmax, nd, d);
+            for (int s2 = 0; s2 < nd; ++s2) planes[(size_t)s2 * KK * RH + (size_t)j * RH + kk] = half_of_int(d[s2]);
         }
     }
+}
+
+// FP32 value rounded to TF32 (10 fraction bits), nearest with ties away from
+// zero, as a float; infinities and NaNs pass through.
+static float tf32_round(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7F800000u) != 0x7F800000u) u = (u + 0x1000u) & 0xFFFFE000u;
+    float r;
+    std::memcpy(&r, &u, 4);
+    return r;
+}
+
+// 3xTF32 form of a complex gate: the interleaved real B of convert_tc, each
+// entry split into hi = tf32(b), lo = tf32(b - hi), stored in m16n8k8
+// B-fragment order (k-step ks, n-tile nt, lane l: {hi b0, hi b1, lo b0,
+// lo b1}, b0 = B[8ks + l%4][8nt + l/4], b1 = B[8ks + l%4 + 4][8nt + l/4]).
+static void convert_tf32(const GateOp& op, unsigned char* dst) {
+    const int D = 1 << op.k, KK = 2 * D, NT = KK / 8;
+    auto bval = [&](int kk, int j) -> double {
+        const cplx m = op.m[(size_t)(j >> 1) * D + (kk >> 1)];
+        const int pin = kk & 1, pout = j & 1;
+        if (pin == 0) return pout == 0 ? m.real() : m.imag();
+        return pout == 0 ? -m.imag() : m.real();
+    };
+    float* out = reinterpret_cast<float*>(dst);
+    for (int ks = 0; ks < NT; ++ks)
+        for (int nt = 0; nt < NT; ++nt)
+            for (int l = 0; l < 32; ++l) {
+                const int n = nt * 8 + l / 4, k0 = ks * 8 + l % 4;
+                const double b0 = bval(k0, n), b1 = bval(k0 + 4, n);
+                const float h0 = tf32_round((float)b0), h1 = tf32_round((float)b1);
+                float* f = out + ((size_t)(ks * NT + nt) * 32 + l) * 4;
+                f[0] = h0;
+                f[1] = h1;
+                f[2] = tf32_round((float)(b0 - (double)h0));
+                f[3] = tf32_round((float)(b1 - (double)h1));
+            }
+}
+
+static void convert_tc_any(int arith, const GateOp& op, unsigned char* dst) {
+    if (arith == kArithTF32) convert_tf32(op, dst);
+    else convert_tc(op, tc_digits_b(arith), dst);
 }
 
 // Dense gates are stored transposed (element c * dim + r holds M[r][c]): the
@@ -324,20 +381,20 @@ size_t pass_pool_bytes(int arith, const PassDesc& d) {
     return ((size_t)d.mat_elems * Workspace::mat_elem_bytes(arith) + 255) & ~(size_t)255;
 }
 
-std::shared_ptr<const std::vector<unsigned char>> make_tc_pool(const GateOp& op) {
-    auto v = std::make_shared<std::vector<unsigned char>>(tc_pool_bytes(op.k));
-    convert_tc(op, v->data());
+std::shared_ptr<const std::vector<unsigned char>> make_tc_pool(int arith, const GateOp& op) {
+    auto v = std::make_shared<std::vector<unsigned char>>(tc_pool_bytes(arith, op.k));
+    convert_tc_any(arith, op, v->data());
     return v;
 }
 
 void write_pass_pool(int arith, const PassDesc& d, const GateOp* ops, unsigned char* dst) {
-    size_t off = 0;
+    const size_t melem = Workspace::mat_elem_bytes(arith);
     for (int o = 0; o < d.nops; ++o) {
+        unsigned char* p = dst + (size_t)d.ops[o].mat_off * melem;
         const bool tc = d.ops[o].tc != 0;
-        if (tc && ops[o].tc_pool) std::memcpy(dst + off, ops[o].tc_pool->data(), ops[o].tc_pool->size());
-        else if (tc) convert_tc(ops[o], dst + off);
-        else convert_matrix(arith, ops[o], dst + off);
-        off += pool_elems(arith, ops[o], tc) * Workspace::mat_elem_bytes(arith);
+        if (tc && ops[o].tc_pool) std::memcpy(p, ops[o].tc_pool->data(), ops[o].tc_pool->size());
+        else if (tc) convert_tc_any(arith, ops[o], p);
+        else convert_matrix(arith, ops[o], p);
     }
 }
 
@@ -357,14 +414,7 @@ uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<G
     unsigned char* host = static_cast<unsigned char*>(pinned_);
     for (size_t pi = 0; pi < plans.size(); ++pi) {
         const PassPlan& p = plans[pi];
-        size_t off = p.pool_off;
-        for (int o = 0; o < p.desc.nops; ++o) {
-            const GateOp& op = ops[first[pi] + o];
-            const bool tc = p.desc.ops[o].tc != 0;
-            if (tc) convert_tc(op, host + off);
-            else convert_matrix(arith, op, host + off);
-            off += pool_elems(arith, op, tc) * mat_elem_bytes(arith);
-        }
+        write_pass_pool(arith, p.desc, ops.data() + first[pi], host + p.pool_off);
     }
     cuda_check(cudaMemcpyAsync(pool_, pinned_, total, cudaMemcpyHostToDevice, stream_), "cudaMemcpyAsync(matrices)");
     cuda_check(cudaEventRecord(staging_free_, stream_), "cudaEventRecord");

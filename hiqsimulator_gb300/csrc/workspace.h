@@ -62,7 +62,7 @@ public:
     // workspace (reused between calls; valid until the next upload).
     void* upload(const void* host, size_t bytes);
 
-    static size_t mat_elem_bytes(int arith) { return arith == kArithF32 ? 8 : 16; }
+    static size_t mat_elem_bytes(int arith) { return arith_is_c64(arith) ? 8 : 16; }
 
     // Per-launch device timing of the apply passes (CUDA events around each
     // launch on the workspace stream). collect_timing() waits for the events,
@@ -114,6 +114,6 @@ inline std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<Gat
     return plan_passes(n, arith, ops.data(), ops.size(), max_tile_bits, max_ops, op_first);
 }
 // The tensor-core pool bytes of a dense gate (k >= 3), for GateOp::tc_pool.
-std::shared_ptr<const std::vector<unsigned char>> make_tc_pool(const GateOp& op);
+std::shared_ptr<const std::vector<unsigned char>> make_tc_pool(int arith, const GateOp& op);
 
 }  // namespace hqs

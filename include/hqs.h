@@ -46,6 +46,13 @@ extern "C" {
 #define HQS_ARITH_F32 3  /* FP32 (complex64 states) */
 #define HQS_ARITH_TC 4   /* complex128: dense 3-5 qubit gates as exact fp16 digit products on the
                             tensor cores, everything else double-float */
+#define HQS_ARITH_TF32 5 /* complex64: dense 3-5 qubit gates as 3xTF32 products on the tensor
+                            cores (hi*hi + hi*lo + lo*hi, FP32 accumulate), everything else FP32.
+                            The tensor cores' accumulation rounds toward zero: the state's norm
+                            shrinks by about 1e-7 per dense gate (measured). */
+#define HQS_ARITH_TC64 6 /* complex64: dense 3-5 qubit gates as exact two-digit fp16 products on
+                            the tensor cores (round to nearest, no norm drift), everything else
+                            FP32. hqs_sim / hqs_server map HQS_ARITH_TC with HQS_C64 to this. */
 
 typedef struct hqs_sim hqs_sim;
 
@@ -209,8 +216,8 @@ int hqs_server_info(const hqs_server* srv, uint64_t out[5]);
 
 /* ------------------------------------------------------------------------
  * Kernel-level API on device memory (one fused gate / reduction per call).
- * state: device pointer to 2^n amplitudes (complex128 for HQS_ARITH_F64/DF,
- * complex64 for HQS_ARITH_F32). stream: a cudaStream_t or NULL. Calls are
+ * state: device pointer to 2^n amplitudes (complex128 for HQS_ARITH_F64/DF/TC,
+ * complex64 for HQS_ARITH_F32/TF32/TC64). stream: a cudaStream_t or NULL. Calls are
  * asynchronous except those returning a value to the host.
  * ------------------------------------------------------------------------ */
 typedef struct hqs_ws hqs_ws;

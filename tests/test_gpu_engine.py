@@ -420,20 +420,33 @@ def test_move_qubits_keeps_every_query(make):
     assert sim.get_amplitude([bool((0x5A5A >> q) & 1) for q in qs], qs) == amp
 
 
-def test_c64_fidelity_against_c128_oracle(hqs, cuda):
+@pytest.mark.parametrize("arith", ["f32", "tc", "tf32"])
+def test_c64_fidelity_against_c128_oracle(hqs, cuda, arith):
+    """complex64 against the FP64 oracle: fidelity >= 1 - 1e-6. The 3xTF32
+    mode rounds toward zero in the tensor cores' accumulation, so its state
+    keeps its direction (normalized fidelity) but loses norm (about 6e-7 per
+    dense gate, 29 here); it is held to the normalized fidelity and a norm
+    bound."""
     from hiqsimulator_gb300 import circuits
     from oracle.engine import OracleSimulator
     n = 18
     qs = list(range(n))
     gates = circuits.brickwork(8, qs, 20)
     cmds = circuits.greedy_stream(gates, qs, 5)
-    sim = hqs.SimulatorMPI(8, 24, 5, "c64")
+    sim = hqs.SimulatorMPI(8, 24, 5, "c64", arith)
+    assert sim.arith == arith
     ref = OracleSimulator(8, 24, 5)
     for s in (sim, ref):
         s.allocate_qureg(qs, 0)
         circuits.replay(s, cmds)
         s.run()
     _, vec = sim.cheat_local_numpy()
+    norm = np.vdot(vec, vec).real
     fid = abs(np.vdot(ref.vec, vec)) ** 2
-    assert fid > 1 - 1e-6, fid
+    if arith == "tf32":
+        assert fid / norm > 1 - 1e-9, fid / norm
+        assert abs(norm - 1) < 1e-4, norm
+    else:
+        assert fid > 1 - 1e-6, fid
+        assert abs(norm - 1) < 1e-6, norm
     assert np.max(np.abs(vec - ref.vec)) < 1e-5

@@ -9,6 +9,14 @@ pytestmark = pytest.mark.gpu
 
 C128_TOL = 1e-12   # max-abs, complex128 states (F64 and DF arithmetic)
 C64_TOL = 2e-6     # max-abs, complex64 states of norm 1
+C64_ARITH = ("f32", "tf32", "tc64")
+TC64_REL = 2e-5    # two-digit tensor-core gates: max-abs error over the largest amplitude
+
+
+def tol(arith, ref, scale=1.0):
+    if arith == "tc64":
+        return scale * TC64_REL * float(np.max(np.abs(ref)))
+    return scale * (C64_TOL if arith in C64_ARITH else C128_TOL)
 
 
 def rand_state(rng, n):
@@ -67,7 +75,7 @@ def ws(hqs, cuda):
     w.close()
 
 
-@pytest.mark.parametrize("arith", ["f64", "df", "tc", "f32"])
+@pytest.mark.parametrize("arith", ["f64", "df", "tc", "f32", "tf32", "tc64"])
 @pytest.mark.parametrize("n", [1, 3, 6, 11, 14])
 def test_single_gates_match_oracle(ws, cuda, oracle_lib, arith, n):
     rng = np.random.Generator(np.random.PCG64(1000 + n))
@@ -75,16 +83,16 @@ def test_single_gates_match_oracle(ws, cuda, oracle_lib, arith, n):
         for diag in (False, True):
             gate = rand_gate(rng, n, k, diag=diag)
             psi = rand_state(rng, n)
-            d = Dev(cuda, psi, c64=(arith == "f32"))
+            d = Dev(cuda, psi, c64=arith in C64_ARITH)
             ws.apply_gates(d.ptr, n, arith, [gate])
             ws.synchronize()
             ref = psi.copy()
             oracle_apply(oracle_lib, ref, gate)
             err = np.max(np.abs(d.host() - ref))
-            assert err < (C64_TOL if arith == "f32" else C128_TOL), (arith, n, k, diag, err)
+            assert err < tol(arith, ref), (arith, n, k, diag, err)
 
 
-@pytest.mark.parametrize("arith", ["f64", "df", "tc", "f32"])
+@pytest.mark.parametrize("arith", ["f64", "df", "tc", "f32", "tf32", "tc64"])
 @pytest.mark.parametrize("n,tile", [(12, 11), (16, 11), (16, 8), (20, 12)])
 def test_fused_passes_match_sequential_oracle(ws, cuda, oracle_lib, arith, n, tile):
     """Many gates planned into multi-gate tiled passes equal the gates applied
@@ -98,7 +106,7 @@ def test_fused_passes_match_sequential_oracle(ws, cuda, oracle_lib, arith, n, ti
         else:
             gates.append(rand_gate(rng, n, k, diag=bool(rng.random() < 0.3)))
     psi = rand_state(rng, n)
-    d = Dev(cuda, psi, c64=(arith == "f32"))
+    d = Dev(cuda, psi, c64=arith in C64_ARITH)
     by, passes = ws.apply_gates(d.ptr, n, arith, gates, max_tile_bits=tile)
     ws.synchronize()
     assert 1 <= passes <= len(gates)
@@ -106,7 +114,7 @@ def test_fused_passes_match_sequential_oracle(ws, cuda, oracle_lib, arith, n, ti
     for g in gates:
         oracle_apply(oracle_lib, ref, g)
     err = np.max(np.abs(d.host() - ref))
-    assert err < (5 * C64_TOL if arith == "f32" else C128_TOL), (arith, n, err, passes)
+    assert err < tol(arith, ref, 5.0 if arith in C64_ARITH else 1.0), (arith, n, err, passes)
 
 
 @pytest.mark.parametrize("arith", ["f64", "df", "f32"])

@@ -28,17 +28,17 @@ def _mix(seed, count, nmax=14):
     return serving.serving_workload(seed, count, nmin=6, nmax=nmax, dmin=3, dmax=12)
 
 
-@pytest.mark.parametrize("precision", ["c128", "c64"])
-def test_result_alone_equals_result_in_mix(hqs, cuda, precision):
+@pytest.mark.parametrize("precision,arith", [("c128", "auto"), ("c64", "f32"), ("c64", "tc"), ("c64", "tf32")])
+def test_result_alone_equals_result_in_mix(hqs, cuda, precision, arith):
     from hiqsimulator_gb300 import serving
     circuits = _mix(11, 24)
     alone = {}
     for idx in (0, 5, 9, 17):
-        srv = serving.Server(precision, budget_bytes=1 << 30)
+        srv = serving.Server(precision, arith, budget_bytes=1 << 30)
         srv.submit(circuits[idx])
         alone[idx] = srv.drain()[0]
         srv.close()
-    srv = serving.Server(precision, budget_bytes=1 << 30)
+    srv = serving.Server(precision, arith, budget_bytes=1 << 30)
     ids = {srv.submit(c): i for i, c in enumerate(circuits)}
     mixed = {ids[r["id"]]: r for r in srv.drain()}
     assert len(mixed) == len(circuits)
