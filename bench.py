@@ -4,10 +4,13 @@ is quoted on: 30-qubit complex128 state (16 GiB), QFT on all 30 qubits
 followed by 10 seeded random layers (Haar U(2) on every qubit, CNOTs on a
 random perfect matching, one controlled phase), greedy fusion k <= 5.
 
-A step applies the whole fused circuit to the resident state. The metric is
-the reference-equivalent state bandwidth: every fused gate of the greedy
-schedule is one sweep of the reference engine (kernelK, 2 * 2^n * 16 bytes,
-halved per control), so value = sum of those bytes / step time. Inputs are
+A step applies the whole fused circuit to the resident state and then forces
+one qubit permutation (the qubits at the top 5 positions move to positions
+0-4: one in-HBM bit-permutation sweep, standing in for the reference's
+global/local qubit swap). The metric is the reference-equivalent state
+bandwidth: every fused gate of the greedy schedule is one sweep of the
+reference engine (kernelK, 2 * 2^n * 16 bytes, halved per control) and the
+permutation one more, so value = sum of those bytes / step time. Inputs are
 larger than L2 (16 GiB state), so no flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -77,7 +80,7 @@ class Dist:
 
 def workload():
     from hiqsimulator_gb300 import circuits
-    gates = circuits.config1(seed=SEED, n=N_QUBITS, layers=10)
+    gates = circuits.qft_random_layers(seed=SEED, n=N_QUBITS, layers=10)
     t0 = time.time()
     clusters = circuits.greedy_clusters(gates, list(range(N_QUBITS)), CLUSTER)
     log("schedule: %d gates -> %d fused gates in %.1fs" % (len(gates), len(clusters), time.time() - t0))
@@ -193,15 +196,58 @@ def cpu_sample(cmds, clusters, max_gates, budget_s):
         done, t_total)
 
 
+def force_permutation(sim):
+    """Move the qubits at the top 5 positions to positions 0-4 (one sweep)."""
+    top = sim.get_qubits_ids()[-5:]
+    sim.move_qubits(top, list(range(5)))
+
+
+def capacity_report():
+    """The largest states one GPU holds: 33 qubits complex128 and 34 qubits
+    complex64 (128 GiB each). Random layers with CNOT targets biased to the
+    top 8 qubits + 4 Grover iterations (multi-controlled Z over all qubits),
+    gates sent one run() each (the engine's pass planner tiles them); timed
+    forward, then the inverse circuit must return |0...0>."""
+    import hiqsimulator_gb300 as hqs
+    from hiqsimulator_gb300 import circuits
+    out = {}
+    for prec, n in (("c128", 33), ("c64", 34)):
+        gates, _ = circuits.capacity_circuit(seed=99, n=n)
+        qs = list(range(n))
+        sim = hqs.SimulatorMPI(99, n, 5, prec)
+        sim.allocate_qureg(qs, 0)
+        sim.synchronize()
+        sim.enable_pass_timing(True)
+        sim.timer_start()
+        circuits.replay(sim, circuits.fusion_off_stream(gates))
+        ms = sim.timer_stop()
+        pt = sim.pass_timing()
+        sim.enable_pass_timing(False)
+        norm = sim.get_probability([], [])
+        circuits.replay(sim, circuits.fusion_off_stream(circuits.inverse(gates)))
+        p0 = abs(sim.get_amplitude([False] * n, qs)) ** 2
+        out[prec] = {"qubits": n, "state_bytes": (16 if prec == "c128" else 8) << n, "gates": len(gates),
+                     "ms": ms, "passes": pt["launches"], "pass_bytes": pt["bytes"],
+                     "pass_GBs": pt["bytes"] / (pt["ms"] / 1e3) / 1e9 if pt["ms"] > 0 else None,
+                     "norm_after_circuit": norm, "round_trip_p0": p0}
+        log("capacity %s %dq: %d gates in %.0f ms (%d passes, %.0f GB/s in passes), norm-1 %.1e, "
+            "1-p0 after inverse %.1e" % (prec, n, len(gates), ms, pt["launches"], out[prec]["pass_GBs"] or 0,
+                                         norm - 1, 1 - p0))
+        del sim
+    return out
+
+
 def serving_report(args):
-    """Config-4-style serving (smaller count): Poisson arrivals of circuits with
-    n ~ U{10..22}, depth ~ U{10..60}; batched continuous serving against the
-    same server running one circuit per launch."""
+    """Serving of many small circuits: Poisson arrivals of circuits with
+    n ~ U{10..22}, depth ~ U{10..60} random layers; batched continuous
+    serving in each precision, and (complex128, first rate) against the same
+    server running one circuit per launch."""
     from hiqsimulator_gb300 import serving
     out = {"circuits": args.serve, "budget_bytes": int(150e9),
            "workload": "n~U{10..22}, depth~U{10..60} random layers; 30% sample, 20% 8-term <H>, 50% <0|psi>"}
     circuits = serving.serving_workload(2024, args.serve)
-    for prec, arith, key in (("c128", "auto", "c128"), ("c64", "f32", "c64_f32"), ("c64", "tf32", "c64_tf32")):
+    for prec, arith, key in (("c128", "tc", "c128"), ("c64", "tc", "c64_tc"), ("c64", "f32", "c64_f32"),
+                             ("c64", "tf32", "c64_tf32")):
         rep = {}
         for rate in args.serve_rates:
             arr = serving.poisson_arrivals(2024, len(circuits), rate)
@@ -292,8 +338,8 @@ def run_ours(args, dist):
     import hiqsimulator_gb300 as hqs
     from hiqsimulator_gb300 import circuits
     gates, clusters, cmds = workload()
-    ref_bytes = cluster_bytes(gates, clusters)
-    zz, shots = circuits.config1_observables(SEED, N_QUBITS)
+    ref_bytes = cluster_bytes(gates, clusters) + 2 * (16 << N_QUBITS)  # + the forced permutation
+    zz, shots = circuits.zz_pairs_and_shots(SEED, N_QUBITS)
     ids = list(range(N_QUBITS))
 
     # ---- device-resident timing (value): state allocated once, steps replay the
@@ -304,6 +350,7 @@ def run_ours(args, dist):
     sim.synchronize()
     for _ in range(args.warmup):
         circuits.replay(sim, cmds)
+        force_permutation(sim)
         sim.synchronize()
     clocks = ClockSampler(dist.local)
     dist.barrier()
@@ -313,6 +360,7 @@ def run_ours(args, dist):
     sim.timer_start()
     for _ in range(args.steps):
         circuits.replay(sim, cmds)
+        force_permutation(sim)
     ms = sim.timer_stop()
     pt = sim.pass_timing()
     sim.enable_pass_timing(False)
@@ -320,7 +368,7 @@ def run_ours(args, dist):
     s1 = sim.stats()
     ms = dist.max(ms)
     dist.barrier()
-    launches = s1["passes"] - s0["passes"]
+    launches = s1["passes"] - s0["passes"] + args.steps  # fused passes + one permutation per step
     value = dist.ws * args.steps * ref_bytes / (ms / 1e3) / 1e9
     log("value: %.1f GB/s over %d steps (%.1f ms/step, %d launches)" % (value, args.steps, ms / args.steps, launches))
 
@@ -343,6 +391,7 @@ def run_ours(args, dist):
         s.allocate_qureg(ids, 0)
         circuits.replay(s, cmds)
         s.run()
+        force_permutation(s)
         ev = [s.get_expectation_value([([(a, "Z"), (b, "Z")], 1.0)], ids) for a, b in zz]
         smp = s.sample(shots)
         return ev, smp
@@ -369,6 +418,7 @@ def run_ours(args, dist):
 
     serv = serving_report(args) if (dist.rank == 0 and args.serve > 0) else None
     prec = precision_report() if (dist.rank == 0 and not args.no_precision) else None
+    cap = capacity_report() if (dist.rank == 0 and args.capacity) else None
 
     if dist.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
@@ -378,10 +428,11 @@ def run_ours(args, dist):
                 "config": {"workload": "QFT%d + 10 random layers, greedy fusion k<=5, complex128, %d qubits" % (
                                N_QUBITS, N_QUBITS),
                            "fused_gates_per_step": len(clusters), "gates_per_step": len(gates),
+                           "forced_permutation": "top 5 qubits to positions 0-4 once per step",
                            "state_bytes": 16 << N_QUBITS, "l2": "inputs larger than L2 (16 GiB state)",
                            "parallelism": "replicas" if dist.ws > 1 else "single GPU"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk, "serving": serv, "precision": prec}
+                "clocks": clk, "serving": serv, "precision": prec, "capacity": cap}
         print(json.dumps(line), flush=True)
     return 0
 
@@ -401,6 +452,7 @@ def main():
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[4000.0, 400.0])
     ap.add_argument("--serve-slots", type=int, default=32, help="resident circuits at most while serving")
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--capacity", action="store_true", help="also run the 33q c128 / 34q c64 capacity states")
     args = ap.parse_args()
     global N_QUBITS
     N_QUBITS = args.qubits

@@ -158,18 +158,19 @@ def replay(sim, cmds):
 
 # ------------------------------------------------------------ configurations
 
-def config0(seed=1234, n=20, layers=20):
+def random_circuit_20q(seed=1234, n=20, layers=20):
     """20-qubit seeded random circuit (20 layers)."""
     return random_layers(seed, list(range(n)), layers)
 
 
-def config1(seed=4321, n=30, layers=10):
+def qft_random_layers(seed=4321, n=30, layers=10):
     """QFT on all n qubits followed by `layers` random layers."""
     qs = list(range(n))
     return qft(qs) + random_layers(seed, qs, layers)
 
 
-def config1_observables(seed, n, pairs=64, shots=1024):
+def zz_pairs_and_shots(seed, n, pairs=64, shots=1024):
+    """Seeded qubit pairs for <Z_i Z_j> and the number of full-register samples."""
     rng = rng_for(seed + 7)
     zz = []
     for _ in range(pairs):
@@ -178,7 +179,10 @@ def config1_observables(seed, n, pairs=64, shots=1024):
     return zz, shots
 
 
-def config2(seed=99, n=33, layers=8, grover=4):
+def capacity_circuit(seed=99, n=33, layers=8, grover=4):
+    """Random layers with CNOT targets biased 70% towards the top 8 qubits,
+    then Grover iterations (multi-controlled Z on all n qubits) for a seeded
+    marked string. Returns (gates, marked)."""
     qs = list(range(n))
     top = set(qs[-8:])
     g = random_layers(seed, qs, layers, cnot_target_pool=top, bias=0.7)
@@ -186,8 +190,13 @@ def config2(seed=99, n=33, layers=8, grover=4):
     return g + gr, marked
 
 
-def config3(seed=2024, n=28, layers=40):
+def brickwork_28q(seed=2024, n=28, layers=40):
     return brickwork(seed, list(range(n)), layers)
+
+
+def inverse(gates):
+    """The inverse circuit: reversed order, conjugate-transposed matrices."""
+    return [Gate(np.conj(np.asarray(g.matrix)).T.copy(), list(g.ids), list(g.ctrls)) for g in reversed(gates)]
 
 
 def pauli_sum(seed, n, terms=8):

@@ -32,7 +32,7 @@ Engine::Engine(uint64_t seed, int64_t max_local, int64_t max_cluster_size, int p
       max_local_(max_local),
       max_cluster_(max_cluster_size),
       rnd_eng_(seed) {
-    if (arith_ == 0) arith_ = (precision_ == kC64) ? kArithF32 : kArithTC;
+    if (arith_ == 0) arith_ = (precision_ == kC64) ? kArithTC64 : kArithTC;
     if (precision_ == kC64 && arith_ == kArithTC) arith_ = kArithTC64;  // tensor-core digits, two per real
     if (precision_ == kC64 && !arith_is_c64(arith_)) fail("complex64 states use F32 or TF32 arithmetic");
     if (precision_ == kC128 && arith_is_c64(arith_)) fail("complex128 states use F64, DF or TC arithmetic");

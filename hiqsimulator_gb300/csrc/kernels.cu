@@ -247,27 +247,15 @@ __device__ __forceinline__ void digits5(double v, int ebrow, int (&d)[kTcDigits]
     d[4] = (r4 ^ sg) - sg;
 }
 
-// Two digits of an FP32 v relative to its row's largest biased exponent
-// ebrow (|v| < 2^(ebrow - 126)): X = round(|v| 2^(19-E_row)) <= 2^19 (to
-// nearest, ties to even) is cut into two 10-bit fields, balanced into
-// [-512, 511] (the top one into [-512, 512]) with a carry, then given v's
-// sign.
-__device__ __forceinline__ void digits2(float v, int ebrow, int (&d)[2]) {
-    const uint32_t u = __float_as_uint(v);
-    const int eb = (int)((u >> 23) & 0xFFu);
-    uint32_t a = 0;
-    const int sh = 5 + ebrow - eb;  // >= 5
-    if (eb != 0 && sh < 32) {
-        const uint32_t M = (u & 0x7FFFFFu) | 0x800000u;
-        a = (M + (1u << (sh - 1)) - 1u + ((M >> sh) & 1u)) >> sh;
-    }
-    int r1 = (int)(a & 1023u), r0 = (int)(a >> 10);
-    const int c = (r1 + 512) >> 10;
-    r1 -= c << 10;
-    r0 += c;
-    const int sg = (int)(u >> 31) ? -1 : 0;
-    d[0] = (r0 ^ sg) - sg;
-    d[1] = (r1 ^ sg) - sg;
+// Two digits of an FP32 v on the FP32 pipe. s = 2^(19 - E_row) with
+// |v| < 2^E_row (s = 0 flushes rows below 2^-106). Adding 1.5 * 2^23 rounds
+// to an integer (to nearest, ties to even): X = rint(v s), |X| <= 2^19, then
+// hi = rint(X / 1024) and lo = X - 1024 hi, both in [-512, 512] and exact.
+constexpr float kRoundMagic = 12582912.0f;  // 1.5 * 2^23
+__device__ __forceinline__ void digits2f(float v, float s, float& hi, float& lo) {
+    const float x = __fadd_rn(__fmaf_rn(v, s, kRoundMagic), -kRoundMagic);
+    hi = __fadd_rn(__fmaf_rn(x, 1.0f / 1024.0f, kRoundMagic), -kRoundMagic);
+    lo = __fmaf_rn(hi, -1024.0f, x);
 }
 
 // S * 2^sc as the nearest double (ties away from zero), built from bits.
@@ -358,6 +346,7 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
     const __half* planeB = reinterpret_cast<const __half*>(pool + 4 * KK);
     __half* planeA = reinterpret_cast<__half*>(scratch);
     int* erow = reinterpret_cast<int*>(scratch + (size_t)ND * G * RH * 2);
+    // complex128: int32 E_col per column; complex64: float 2^(E_col - 19)
 
     int ss[K];
     uint32_t bitv[K];
@@ -421,16 +410,21 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
 #pragma unroll
         for (int u = 0; u < CPI; ++u) {
             const V x = src[Lb + offset_of(ch * CPI + u)];
-            int dr[ND], di[ND];
             if constexpr (kC128) {
+                int dr[ND], di[ND];
                 digits5(x.x, ebrow, dr);
                 digits5(x.y, ebrow, di);
-            } else {
-                digits2(x.x, ebrow, dr);
-                digits2(x.y, ebrow, di);
-            }
 #pragma unroll
-            for (int sdx = 0; sdx < ND; ++sdx) w[sdx][u] = pack_digits(dr[sdx], di[sdx]);
+                for (int sdx = 0; sdx < ND; ++sdx) w[sdx][u] = pack_digits(dr[sdx], di[sdx]);
+            } else {
+                const float s = ebrow >= 20 ? __int_as_float((272 - ebrow) << 23) : 0.f;
+                float hr, lr, hi, li;
+                digits2f(x.x, s, hr, lr);
+                digits2f(x.y, s, hi, li);
+                __half2 h0 = __floats2half2_rn(hr, hi), h1 = __floats2half2_rn(lr, li);
+                w[0][u] = *reinterpret_cast<uint32_t*>(&h0);
+                w[1][u] = *reinterpret_cast<uint32_t*>(&h1);
+            }
         }
 #pragma unroll
         for (int sdx = 0; sdx < ND; ++sdx)
@@ -510,18 +504,19 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
                 }
                 dst[idx] = make_double2(outv[0], outv[1]);
             } else {
-                const int er = erow[g] - 126;
+                // accumulators hold exact integers: value = (L0 2^20 + L1 2^10
+                // + L2) * 2^(E_row - 19) * 2^(E_col - 19), the last factor
+                // stored per column in the pool as a float
+                const int eb = erow[g];
+                const float rs = eb >= 20 ? __int_as_float((eb - 18) << 23) : 0.f;
+                const float* cscale = reinterpret_cast<const float*>(ecol);
                 float outv[2];
 #pragma unroll
                 for (int c2 = 0; c2 < 2; ++c2) {
-                    // S = L0 2^20 + L1 2^10 + L2 (< 2^45),
-                    // value = S * 2^(E_row + E_col - 38)
                     const int e = h * 2 + c2;
-                    const long long L0 = __float2int_rn(acc[0][e]);
-                    const long long L1 = (long long)__float2int_rn(acc[1][e]) + __float2int_rn(acc[2][e]);
-                    const long long L2 = __float2int_rn(acc[3][e]);
-                    const long long S = (L0 << 20) + (L1 << 10) + L2;
-                    outv[c2] = ldexpf(__ll2float_rn(S), er + ecol[nt * 8 + tig * 2 + c2] - 38);
+                    const float S = __fmaf_rn(acc[0][e], 1048576.0f,
+                                              __fmaf_rn(__fadd_rn(acc[1][e], acc[2][e]), 1024.0f, acc[3][e]));
+                    outv[c2] = __fmul_rn(__fmul_rn(S, rs), cscale[nt * 8 + tig * 2 + c2]);
                 }
                 dst[idx] = make_float2(outv[0], outv[1]);
             }

@@ -49,7 +49,7 @@ int parse_arith(const std::string& a) {
     if (a == "tc") return HQS_ARITH_TC;
     if (a == "tf32") return HQS_ARITH_TF32;
     if (a == "tc64") return HQS_ARITH_TC64;
-    throw py::value_error("arith must be 'auto', 'f64', 'df', 'tc', 'f32' or 'tf32'");
+    throw py::value_error("arith must be 'auto', 'f64', 'df', 'tc', 'f32', 'tf32' or 'tc64'");
 }
 
 std::string env_or(const char* name, const char* dflt) {

@@ -42,7 +42,7 @@ Server::Server(int precision, int arith, uint64_t budget_bytes, int max_active, 
       max_active_(std::max(1, max_active)),
       cluster_(std::max(1, std::min(cluster_size, kMaxK))),
       budget_(budget_bytes) {
-    if (arith_ == 0) arith_ = precision_ == 1 ? kArithF32 : kArithTC;
+    if (arith_ == 0) arith_ = precision_ == 1 ? kArithTC64 : kArithTC;
     if (precision_ == 1 && arith_ == kArithTC) arith_ = kArithTC64;
     if ((precision_ == 1) != arith_is_c64(arith_)) throw std::invalid_argument("server: precision/arith mismatch");
     for (int i = 0; i < 2; ++i) cuda_check(cudaEventCreateWithFlags(&staging_done_[i], cudaEventDisableTiming), "cudaEventCreate");
@@ -134,7 +134,7 @@ uint64_t Server::submit(int n, const std::vector<ServerGate>& gates, int kind, d
     // digit planes of tensor-core-sized gates once, not every round
     if (arith_has_tc(arith_))
         for (auto& op : r.ops)
-            if (op.k >= 3 && !op.diag) op.tc_pool = make_tc_pool(arith_, op);
+            if (tc_candidate(arith_, op)) op.tc_pool = make_tc_pool(arith_, op);
     queue_.push_back(std::move(r));
     return queue_.back().id;
 }

@@ -113,7 +113,13 @@ static size_t tc_scratch_bytes(int arith, int q, int k) {
     return (size_t)tc_digits(arith) * G * (KK + 8) * 2 + 4 * G;
 }
 
-static bool tc_candidate(int arith, const GateOp& op) { return arith_has_tc(arith) && !op.diag && op.k >= 3; }
+// Dense gates that run on the tensor cores: k >= 3 for complex128 (the
+// double-float alternative costs ~10 FP32 operations per real product);
+// k = 5 only for complex64, whose FP32 gates are cheap enough below that
+bool tc_candidate(int arith, const GateOp& op) {
+    if (!arith_has_tc(arith) || op.diag) return false;
+    return op.k >= (arith == kArithTC ? 3 : 5);
+}
 
 // Pool elements (of mat_elem_bytes) an op occupies.
 static size_t pool_elems(int arith, const GateOp& op, bool tc) {
@@ -271,6 +277,9 @@ static void digits_host(double v, int ebmax, int nd, int* d) {
 
 // Real form of a complex gate for the tensor-core path (B with Y = X B, X the
 // interleaved real and imaginary parts of a group's inputs).
+// complex128 (nd = 5): int32 E_col per column. complex64 (nd = 3): the column
+// scale 2^(E_col - 19) as a float, 0 (and no digits) for a column whose
+// largest entry is below 2^-107.
 static void convert_tc(const GateOp& op, int nd, unsigned char* dst) {
     const int D = 1 << op.k, KK = 2 * D, RH = KK + 8;
     // interleaved real form: row 2c + p_in is part p_in of input c, column
@@ -288,6 +297,12 @@ static void convert_tc(const GateOp& op, int nd, unsigned char* dst) {
         int ebmax = 0;
         for (int kk = 0; kk < KK; ++kk) ebmax = std::max(ebmax, biased_exponent(bval(kk, j)));
         ecol[j] = ebmax - 1022;
+        if (nd != kTcDigits) {
+            float sc = 0.f;
+            if (ebmax - 1022 - 19 >= -126) sc = std::ldexp(1.0f, ebmax - 1022 - 19);
+            std::memcpy(&ecol[j], &sc, 4);
+            if (sc == 0.f) continue;
+        }
         for (int kk = 0; kk < KK; ++kk) {
             int d[kTcDigits];
             digits_host(bval(kk, j), ebmax, nd, d);

@@ -113,7 +113,9 @@ inline std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<Gat
                                          int max_ops, std::vector<size_t>* op_first = nullptr) {
     return plan_passes(n, arith, ops.data(), ops.size(), max_tile_bits, max_ops, op_first);
 }
-// The tensor-core pool bytes of a dense gate (k >= 3), for GateOp::tc_pool.
+// Whether the planner runs this gate on the tensor cores (when the tile
+// allows), and the tensor-core pool bytes of such a gate, for GateOp::tc_pool.
+bool tc_candidate(int arith, const GateOp& op);
 std::shared_ptr<const std::vector<unsigned char>> make_tc_pool(int arith, const GateOp& op);
 
 }  // namespace hqs

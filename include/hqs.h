@@ -40,7 +40,7 @@ extern "C" {
 #define HQS_C128 0 /* complex128 state */
 #define HQS_C64 1  /* complex64 state */
 
-#define HQS_ARITH_AUTO 0 /* c128 -> TC, c64 -> F32 */
+#define HQS_ARITH_AUTO 0 /* c128 -> TC, c64 -> TC64 */
 #define HQS_ARITH_F64 1  /* native FP64 */
 #define HQS_ARITH_DF 2   /* double-float (2 x FP32), ~48-bit */
 #define HQS_ARITH_F32 3  /* FP32 (complex64 states) */

@@ -6,7 +6,7 @@ hiqsimulator_gb300.circuits and stores what they return:
 
   ref_states.npz     final states, P(q=1) and measurement outcomes of small
                      circuits (fusion off and greedy fusion), cheat_local order
-  ref_config0.json   20-qubit config-0 summaries (fusion off / greedy k<=4):
+  ref_layers_20q.json   20-qubit random-layer circuit summaries (fusion off / greedy k<=4):
                      P(q=1) for all 20 qubits, the first 64 amplitudes, the
                      amplitudes at 64 seeded indices, sum |a|^2
   ref_sched.json     greedy cluster lists for several circuits
@@ -84,10 +84,10 @@ def main():
         small[name + "_after_meas"] = np.array(sim.cheat_local()[1], dtype=np.complex128)
     np.savez_compressed(os.path.join(HERE, "ref_states.npz"), **small)
 
-    # 20-qubit config 0 summaries
+    # 20-qubit random-layer circuit summaries
     summ = {}
     n = 20
-    gates = circuits.config0(seed=1234, n=n, layers=20)
+    gates = circuits.random_circuit_20q(seed=1234, n=n, layers=20)
     pick = circuits.rng_for(77).choice(1 << n, size=64, replace=False)
     for mode in ("off", "greedy"):
         cmds = stream(gates, n, mode, 4)
@@ -101,7 +101,7 @@ def main():
             "norm": float(np.sum(np.abs(vec) ** 2)),
             "meas": [int(b) for b in sim.measure_qubits(list(range(n)))],
         }
-    with open(os.path.join(HERE, "ref_config0.json"), "w") as f:
+    with open(os.path.join(HERE, "ref_layers_20q.json"), "w") as f:
         json.dump(summ, f)
 
     # schedules

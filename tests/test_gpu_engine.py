@@ -331,11 +331,11 @@ def test_golden_states(make, name, n, layers, mode, K, seed):
 
 
 @pytest.mark.parametrize("mode", ["off", "greedy"])
-def test_golden_config0_20q(make, mode):
+def test_golden_random_layers_20q(make, mode):
     from hiqsimulator_gb300 import circuits
-    ref = json.load(open(os.path.join(GOLDEN, "ref_config0.json")))[mode]
+    ref = json.load(open(os.path.join(GOLDEN, "ref_layers_20q.json")))[mode]
     n = 20
-    gates = circuits.config0(seed=1234, n=n, layers=20)
+    gates = circuits.random_circuit_20q(seed=1234, n=n, layers=20)
     sim = make(1234, 24, 4)
     sim.allocate_qureg(list(range(n)), 0)
     circuits.replay(sim, _stream(gates, n, mode, 4))

@@ -53,10 +53,10 @@ def test_oracle_matches_reference_states(name, n, layers, mode, K, seed):
 
 
 @pytest.mark.parametrize("mode", ["off", "greedy"])
-def test_oracle_matches_reference_config0_20q(mode):
-    ref = json.load(open(os.path.join(GOLDEN, "ref_config0.json")))[mode]
+def test_oracle_matches_reference_random_layers_20q(mode):
+    ref = json.load(open(os.path.join(GOLDEN, "ref_layers_20q.json")))[mode]
     n = 20
-    gates = circuits.config0(seed=1234, n=n, layers=20)
+    gates = circuits.random_circuit_20q(seed=1234, n=n, layers=20)
     sim = _run_oracle(n, _stream(gates, n, mode, 4), 1234, 4)
     p1 = [sim.get_probability([True], [q]) for q in range(n)]
     assert np.max(np.abs(np.array(p1) - ref["p1"])) < TOL
