@@ -24,6 +24,9 @@ int device_sm_count();
 // pass's matrices in the arithmetic's element format. Returns a cudaError_t.
 cudaError_t launch_pass(int arith, void* state, const void* mats, const PassDesc& d, cudaStream_t s);
 size_t pass_smem_bytes(int arith, const PassDesc& d);
+// Resident CTAs per SM the pass kernel for (arith, d) is compiled for (its
+// register budget); shared memory may allow fewer.
+int pass_reg_ctas(int arith, const PassDesc& d);
 
 // One entry of a batched launch: a pass over one state. Device-resident.
 struct BatchItem {

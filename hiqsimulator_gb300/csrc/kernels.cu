@@ -637,6 +637,7 @@ constexpr int kPassGPT = 4;
 
 // Shared-memory layout of a pass (host and device agree through pass_smem_t):
 // [matrix pool][tile A][tile B][high-bit offsets][16-aligned tensor-core scratch]
+// [staging tile, raw state elements, when d.prefetch]
 template <class A>
 struct PassSmem {
     typename A::mat_t* smat;
@@ -644,6 +645,7 @@ struct PassSmem {
     typename A::comp_t* bufB;
     uint64_t* hoff;
     unsigned char* tcs;
+    typename A::store_t* stage;
     __device__ __forceinline__ PassSmem(unsigned char* smem, const PassDesc& d) {
         const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(typename A::mat_t) + 15) & ~(size_t)15;
         const size_t Q = (size_t)1 << d.q;
@@ -653,8 +655,45 @@ struct PassSmem {
         hoff = reinterpret_cast<uint64_t*>(bufB + Q);
         tcs = smem + ((mat_bytes + 2 * sizeof(typename A::comp_t) * Q + sizeof(uint64_t) * ((size_t)1 << (d.q - d.w)) +
                        15) & ~(size_t)15);
+        stage = reinterpret_cast<typename A::store_t*>(tcs + d.tc_bytes);
     }
 };
+
+// Asynchronous global -> shared copies of single state elements (cp.async):
+// each thread copies and later reads back only its own staging slots, so
+// waiting for its own copies is the only synchronisation the staging needs.
+__device__ __forceinline__ void cp_async_elem(double2* sdst, const double2* gsrc) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+                 "l"(gsrc)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_elem(float2* sdst, const float2* gsrc) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(sdst)),
+                 "l"(gsrc)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// First state index of tile t: t's bits spread over the positions outside
+// the tile and the fixed (control) positions, fixed positions set.
+__device__ __forceinline__ uint64_t tile_base(const PassDesc& d, uint64_t t) {
+    uint64_t base = t;
+    for (int i = 0; i < d.nins; ++i) base = insert_zero(base, d.ins_pos[i]);
+    return base | d.fixed_mask;
+}
+
+// Issue this thread's copies of tile t into the staging buffer.
+template <class A>
+__device__ __forceinline__ void tile_prefetch(const typename A::store_t* __restrict__ state, const PassDesc& d,
+                                              const PassSmem<A>& sm, uint64_t t) {
+    const int Q = 1 << d.q;
+    const uint32_t lowmask = (1u << d.w) - 1u;
+    const uint64_t base = tile_base(d, t);
+    for (int L = threadIdx.x; L < Q; L += blockDim.x)
+        cp_async_elem(sm.stage + L, state + base + sm.hoff[L >> d.w] + (L & lowmask));
+    cp_async_commit();
+}
 
 // Stage a pass's matrices and tile offsets into shared memory.
 template <class A>
@@ -671,19 +710,20 @@ __device__ __forceinline__ void pass_setup(const PassSmem<A>& sm, const PassDesc
     __syncthreads();
 }
 
-// One tile of a pass: load, apply the pass's gates in order, store.
+// One tile of a pass: load (unless the caller already placed the tile in
+// bufA), apply the pass's gates in order, store.
 template <class A>
 __device__ __forceinline__ void pass_tile(typename A::store_t* __restrict__ state, const PassDesc& d,
-                                          const PassSmem<A>& sm, uint64_t t) {
+                                          const PassSmem<A>& sm, uint64_t t, bool loaded = false) {
     using C = typename A::comp_t;
     const int Q = 1 << d.q;
     const uint32_t lowmask = (1u << d.w) - 1u;
-    uint64_t base = t;
-    for (int i = 0; i < d.nins; ++i) base = insert_zero(base, d.ins_pos[i]);
-    base |= d.fixed_mask;
-    for (int L = threadIdx.x; L < Q; L += blockDim.x)
-        sm.bufA[L] = A::to_comp(state[base + sm.hoff[L >> d.w] + (L & lowmask)]);
-    __syncthreads();
+    const uint64_t base = tile_base(d, t);
+    if (!loaded) {
+        for (int L = threadIdx.x; L < Q; L += blockDim.x)
+            sm.bufA[L] = A::to_comp(state[base + sm.hoff[L >> d.w] + (L & lowmask)]);
+        __syncthreads();
+    }
     C* src = sm.bufA;
     C* dst = sm.bufB;
     for (int oi = 0; oi < d.nops; ++oi) {
@@ -758,7 +798,22 @@ __global__ void __launch_bounds__(kThreads, pass_min_blocks(A::kId)) pass_kernel
     const PassSmem<A> sm(smem, d);
     pass_setup<A>(sm, d, mats);
     const uint64_t ntiles = 1ULL << (d.n - d.nins);
-    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) pass_tile<A>(state, d, sm, t);
+    if (!d.prefetch) {
+        for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) pass_tile<A>(state, d, sm, t);
+        return;
+    }
+    // software pipeline: tile t + gridDim.x streams into the staging buffer
+    // while tile t is computed
+    const int Q = 1 << d.q;
+    uint64_t t = blockIdx.x;
+    if (t < ntiles) tile_prefetch<A>(state, d, sm, t);
+    for (; t < ntiles; t += gridDim.x) {
+        cp_async_wait_all();
+        for (int L = threadIdx.x; L < Q; L += blockDim.x) sm.bufA[L] = A::to_comp(sm.stage[L]);
+        if (t + gridDim.x < ntiles) tile_prefetch<A>(state, d, sm, t + gridDim.x);
+        __syncthreads();
+        pass_tile<A>(state, d, sm, t, true);
+    }
 }
 
 // Many passes (one per independent state) in one launch: global tile index T
@@ -800,7 +855,7 @@ template <class A>
 size_t pass_smem_t(const PassDesc& d) {
     const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(typename A::mat_t) + 15) & ~(size_t)15;
     return ((mat_bytes + 2 * (sizeof(typename A::comp_t) << d.q) + sizeof(uint64_t) * (1u << (d.q - d.w)) + 15) &
-            ~(size_t)15) + d.tc_bytes;
+            ~(size_t)15) + d.tc_bytes + (d.prefetch ? (sizeof(typename A::store_t) << d.q) : 0);
 }
 
 template <class A>
@@ -1133,6 +1188,18 @@ int device_sm_count() {
 // arithmetic: double-float for complex128, FP32 for complex64.
 static inline int base_arith(int a) {
     return a == kArithTC ? kArithDF : (a == kArithTF32 || a == kArithTC64) ? kArithF32 : a;
+}
+
+int pass_reg_ctas(int arith, const PassDesc& d) {
+    const bool tc = pass_has_tc(d);
+    switch (arith) {
+        case kArithTC: return tc ? pass_min_blocks(ArithDFRaw::kId) : pass_min_blocks(ArithDF::kId);
+        case kArithTC64: return tc ? pass_min_blocks(ArithTC64::kId) : pass_min_blocks(ArithF32::kId);
+        case kArithTF32: return tc ? pass_min_blocks(ArithTF32::kId) : pass_min_blocks(ArithF32::kId);
+        case kArithF64: return pass_min_blocks(ArithF64::kId);
+        case kArithDF: return pass_min_blocks(ArithDF::kId);
+        default: return pass_min_blocks(ArithF32::kId);
+    }
 }
 
 size_t pass_smem_bytes(int arith, const PassDesc& d) {

@@ -260,6 +260,7 @@ std::vector<ServerResult> Server::step() {
         const size_t window = std::min<size_t>(r.ops.size() - r.next, kMaxOpsPerPass);
         std::vector<size_t> first;
         std::vector<PassPlan> plans = plan_passes(r.n, arith_, r.ops.data() + r.next, window, 10, 16, &first, 1);
+        plans[0].desc.prefetch = 0;  // the batched kernel loads its tiles directly
         Planned p{&r, plans[0], r.next, pass_has_tc(plans[0].desc), 0};
         p.smem = pass_smem_bytes(arith_, p.plan.desc);
         r.next += (size_t)plans[0].desc.nops;

@@ -226,6 +226,18 @@ std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t no
         }
         d.mat_elems = moff;
         d.tc_bytes = (uint32_t)((tcb + 15) & ~(size_t)15);
+        // stream the next tile in while computing this one, unless the staging
+        // buffer would cost a resident CTA per SM (228 KB per SM, 1 KB
+        // reserved per CTA, at most 227 KB per CTA)
+        {
+            const int regc = pass_reg_ctas(arith, d);
+            auto ctas = [&](size_t sm) { return std::min<size_t>((size_t)regc, 233472 / (sm + 1024)); };
+            d.prefetch = 0;
+            const size_t s0 = pass_smem_bytes(arith, d);
+            d.prefetch = 1;
+            const size_t s1 = pass_smem_bytes(arith, d);
+            d.prefetch = (s1 <= 232448 && ctas(s1) >= ctas(s0)) ? 1 : 0;
+        }
         pl.pool_off = pool_off;
         pool_off += ((size_t)moff * melem + 255) & ~(size_t)255;
         pl.bytes = 2ULL * (1ULL << (n - popc64(fixed))) * store;
