@@ -188,63 +188,49 @@ __device__ __forceinline__ void apply_dense(const typename A::comp_t* __restrict
 // interleaved real and imaginary parts of each group's inputs (column 2c + p)
 // and B the matching real form of the gate (B[2c][2r] = Re M_rc,
 // B[2c+1][2r] = -Im M_rc, B[2c][2r+1] = Im M_rc, B[2c+1][2r+1] = Re M_rc). Every entry of X is written as
-// 2^E_row * sum_i d_i 2^(-9-10i) with five signed digits |d_i| <= 512 (E_row
-// shared by the row), every entry of B likewise with E_col shared by the
-// column (digits computed on the host). Digits are exact in fp16, a product
+// 2^E_row * sum_i d_i 2^(-8-10i) with five signed digits |d_i| <= 512 (E_row
+// shared by the row, digit_fields5), every entry of B as
+// 2^E_col * sum_j e_j 2^(-9-10j) with E_col shared by the column (digits
+// computed on the host). Digits are exact in fp16, a product
 // of two digits has at most 18 bits and a 2D <= 64 term sum at most 24 bits,
 // so the fp32 accumulation of one digit pair is exact. Pairs (i, j) with
 // i + j <= 2 get their own accumulators, the pairs of levels 3 and 4 share one
-// each (their rounding is below 2^-46 of the row scale), levels >= 5 are
-// dropped (below 2^-47 of it). The epilogue adds the eight accumulators in
-// double-float and re-assembles doubles with integer operations.
+// each, levels >= 5 are dropped (below 2^-46 of the row scale). The epilogue
+// converts the eight accumulators to integers and re-assembles doubles with
+// integer operations.
 
-__device__ __forceinline__ uint32_t pack_digits(int d0, int d1) {
-    const float f0 = __int_as_float(0x4B400000 + d0) - 12582912.0f;
-    const float f1 = __int_as_float(0x4B400000 + d1) - 12582912.0f;
-    __half2 h = __floats2half2_rn(f0, f1);
-    return *reinterpret_cast<uint32_t*>(&h);
-}
-
-// Digits of v relative to the row's largest biased exponent ebrow
-// (|v| < 2^(ebrow - 1022)), most significant first: X = round(|v| 2^(49-E_row))
-// < 2^49 (to nearest, ties to even: ties are frequent when few bits are
-// dropped, and rounding them away from zero would grow the state's norm) is
-// cut into five 10-bit fields, which are balanced into [-512, 511] (the top
-// one into [-512, 512]) with carries, then given v's sign.
-__device__ __forceinline__ void digits5(double v, int ebrow, int (&d)[kTcDigits]) {
+// The five digits of a complex128 state entry v, as biased 10-bit fields:
+// X = round(|v| 2^(48-E_row)) (to nearest, ties to even: ties are frequent
+// when few bits are dropped, and rounding them away from zero would grow the
+// state's norm) with v's sign, |X| <= 2^48, where |v| < 2^E_row,
+// E_row = ebrow - 1022. Y = X + kFieldBias lies in [0, 2^50), and its 10-bit
+// fields f_i (most significant first) give balanced digits d_i = f_i - 512
+// in [-512, 511] with X = sum_i d_i 2^(10(4-i)): no carries, no sign per digit.
+constexpr unsigned long long kFieldBias = 512ULL * (1ULL + (1ULL << 10) + (1ULL << 20) + (1ULL << 30) + (1ULL << 40));
+__device__ __forceinline__ void digit_fields5(double v, int ebrow, uint32_t (&f)[kTcDigits]) {
     const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-    const uint32_t hi = (uint32_t)(u >> 32);
-    const int eb = (int)((hi >> 20) & 0x7FFu);
+    const int eb = (int)((u >> 52) & 0x7FFu);
     unsigned long long a = 0;
-    const int sh = 4 + ebrow - eb;  // >= 4
+    const int sh = 5 + ebrow - eb;  // >= 5
     if (eb != 0 && sh < 62) {
         const unsigned long long M = (u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
         a = (M + (1ULL << (sh - 1)) - 1ULL + ((M >> sh) & 1ULL)) >> sh;
     }
-    const uint32_t alo = (uint32_t)a, ahi = (uint32_t)(a >> 32);
-    int r4 = (int)(alo & 1023u);
-    int r3 = (int)((alo >> 10) & 1023u);
-    int r2 = (int)((alo >> 20) & 1023u);
-    int r1 = (int)(__funnelshift_r(alo, ahi, 30) & 1023u);
-    int r0 = (int)(ahi >> 8);
-    int c = (r4 + 512) >> 10;
-    r4 -= c << 10;
-    r3 += c;
-    c = (r3 + 512) >> 10;
-    r3 -= c << 10;
-    r2 += c;
-    c = (r2 + 512) >> 10;
-    r2 -= c << 10;
-    r1 += c;
-    c = (r1 + 512) >> 10;
-    r1 -= c << 10;
-    r0 += c;
-    const int sg = (int)(hi >> 31) ? -1 : 0;  // negate all digits for negative v
-    d[0] = (r0 ^ sg) - sg;
-    d[1] = (r1 ^ sg) - sg;
-    d[2] = (r2 ^ sg) - sg;
-    d[3] = (r3 ^ sg) - sg;
-    d[4] = (r4 ^ sg) - sg;
+    const unsigned long long Y = ((u >> 63) ? (0ULL - a) : a) + kFieldBias;
+    const uint32_t lo = (uint32_t)Y, hi = (uint32_t)(Y >> 32);
+    f[0] = hi >> 8;
+    f[1] = __funnelshift_r(lo, hi, 30) & 1023u;
+    f[2] = (lo >> 20) & 1023u;
+    f[3] = (lo >> 10) & 1023u;
+    f[4] = lo & 1023u;
+}
+
+// fp16 pair (f0 - 512, f1 - 512) of two biased fields
+__device__ __forceinline__ uint32_t pack_fields(uint32_t f0, uint32_t f1) {
+    const float a = __int_as_float(0x4B3FFE00 + (int)f0) - 12582912.0f;
+    const float b = __int_as_float(0x4B3FFE00 + (int)f1) - 12582912.0f;
+    __half2 h = __floats2half2_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
 }
 
 // Two digits of an FP32 v on the FP32 pipe. s = 2^(19 - E_row) with
@@ -344,9 +330,13 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
     const int G = 1 << (q - K);
     const int* ecol = reinterpret_cast<const int*>(pool);
     const __half* planeB = reinterpret_cast<const __half*>(pool + 4 * KK);
+    // scratch: [ND digit planes of X][erow[G]: row exponents][gbt[G]: first
+    // tile index of each group][offt[D]: tile offset of each input]
     __half* planeA = reinterpret_cast<__half*>(scratch);
     int* erow = reinterpret_cast<int*>(scratch + (size_t)ND * G * RH * 2);
-    // complex128: int32 E_col per column; complex64: float 2^(E_col - 19)
+    uint32_t* gbt = reinterpret_cast<uint32_t*>(erow + G);
+    uint32_t* offt = gbt + G;
+    // pool column scales: complex128 int32 E_col; complex64 float 2^(E_col - 19)
 
     int ss[K];
     uint32_t bitv[K];
@@ -382,15 +372,19 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
     // whenever tile bit 0 is not a target.
     constexpr int CPI = 2;           // complex inputs per item
     constexpr int NCH = D / CPI;     // items per group
-    for (int g = threadIdx.x; g < G; g += blockDim.x) erow[g] = 0;
+    for (int g = threadIdx.x; g < G; g += blockDim.x) {
+        erow[g] = 0;
+        gbt[g] = group_base(g);
+    }
+    for (int c = threadIdx.x; c < D; c += blockDim.x) offt[c] = offset_of(c);
     __syncthreads();
     for (int it = threadIdx.x; it < G * NCH; it += blockDim.x) {
         const int g = it % G, ch = it / G;
-        const uint32_t Lb = group_base(g);
+        const uint32_t Lb = gbt[g];
         int eb = 0;
 #pragma unroll
         for (int u = 0; u < CPI; ++u) {
-            const V x = src[Lb + offset_of(ch * CPI + u)];
+            const V x = src[Lb + offt[ch * CPI + u]];
             if constexpr (kC128) {
                 eb = max(eb, (int)(((unsigned long long)__double_as_longlong(x.x) >> 52) & 0x7FFu));
                 eb = max(eb, (int)(((unsigned long long)__double_as_longlong(x.y) >> 52) & 0x7FFu));
@@ -404,18 +398,18 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
     __syncthreads();
     for (int it = threadIdx.x; it < G * NCH; it += blockDim.x) {
         const int g = it % G, ch = it / G;
-        const uint32_t Lb = group_base(g);
+        const uint32_t Lb = gbt[g];
         const int ebrow = erow[g];
         uint32_t w[ND][CPI];
 #pragma unroll
         for (int u = 0; u < CPI; ++u) {
-            const V x = src[Lb + offset_of(ch * CPI + u)];
+            const V x = src[Lb + offt[ch * CPI + u]];
             if constexpr (kC128) {
-                int dr[ND], di[ND];
-                digits5(x.x, ebrow, dr);
-                digits5(x.y, ebrow, di);
+                uint32_t fr[ND], fi[ND];
+                digit_fields5(x.x, ebrow, fr);
+                digit_fields5(x.y, ebrow, fi);
 #pragma unroll
-                for (int sdx = 0; sdx < ND; ++sdx) w[sdx][u] = pack_digits(dr[sdx], di[sdx]);
+                for (int sdx = 0; sdx < ND; ++sdx) w[sdx][u] = pack_fields(fr[sdx], fi[sdx]);
             } else {
                 const float s = ebrow >= 20 ? __int_as_float((272 - ebrow) << 23) : 0.f;
                 float hr, lr, hi, li;
@@ -474,11 +468,11 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
         // are the real and imaginary parts of output r = nt*4 + tig
         const int gid = lane >> 2, tig = lane & 3;
         const int r = nt * 4 + tig;
-        const uint32_t orow = offset_of(r);
+        const uint32_t orow = offt[r];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const int g = mt * 16 + gid + h * 8;
-            const uint32_t Lb = group_base(g);
+            const uint32_t Lb = gbt[g];
             const uint32_t idx = Lb + orow;
             if ((Lb & op.ctrl_local) != op.ctrl_local) {
                 dst[idx] = src[idx];
@@ -491,7 +485,7 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
                 for (int c2 = 0; c2 < 2; ++c2) {
                     // accumulators hold integers: level sums as one fixed-point
                     // int64 S = L0 2^30 + L1 2^20 + L2 2^10 + L3 + L4 2^-10 (< 2^55),
-                    // value = S * 2^(E_row + E_col - 48)
+                    // value = S * 2^(E_row + E_col - 47)
                     const int e = h * 2 + c2;
                     const long long L0 = __float2int_rn(acc[0][e]);
                     const long long L1 = (long long)__float2int_rn(acc[1][e]) + __float2int_rn(acc[2][e]);
@@ -500,7 +494,7 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
                     const long long L3 = __float2int_rn(acc[6][e]);
                     const long long L4 = __float2int_rn(acc[7][e]);
                     const long long S = (L0 << 30) + (L1 << 20) + (L2 << 10) + L3 + (L4 >> 10);
-                    outv[c2] = fixed_to_double(S, er + ecol[nt * 8 + tig * 2 + c2] - 48);
+                    outv[c2] = fixed_to_double(S, er + ecol[nt * 8 + tig * 2 + c2] - 47);
                 }
                 dst[idx] = make_double2(outv[0], outv[1]);
             } else {

@@ -106,11 +106,12 @@ static size_t tc_pool_bytes(int arith, int k) {
 }
 
 // Shared-memory scratch of a digit-plane gate on a 2^q tile: the tile's
-// digit planes (G = 2^(q-k) rows) and the rows' exponents.
+// digit planes (G = 2^(q-k) rows), the rows' exponents, and the tile
+// offsets of the groups (G) and of the inputs (D).
 static size_t tc_scratch_bytes(int arith, int q, int k) {
     if (arith == kArithTF32) return 0;
     const size_t G = (size_t)1 << (q - k), KK = (size_t)2 << k;
-    return (size_t)tc_digits(arith) * G * (KK + 8) * 2 + 4 * G;
+    return (size_t)tc_digits(arith) * G * (KK + 8) * 2 + 8 * G + 4 * (KK / 2);
 }
 
 // Dense gates that run on the tensor cores: k >= 3 for complex128 (the
