@@ -61,7 +61,8 @@ struct PassDesc {
     uint32_t mat_elems;   // pool elements staged into shared memory
     uint32_t tc_bytes;    // shared-memory scratch for tensor-core digit planes (0: none)
     uint32_t prefetch;    // 1: each CTA copies its next tile into a staging buffer while it
-                          //    computes the current one (cp.async)
+                          //    computes the current one (cp.async); 2: every op works in place,
+                          //    the next tile streams into the second tile buffer
     uint64_t fixed_mask;  // state bits forced to 1 for every processed tile
     uint8_t tile_pos[kMaxTileBits];
     uint8_t ins_pos[64];  // sorted union of tile_pos and fixed-mask positions

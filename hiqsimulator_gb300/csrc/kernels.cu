@@ -315,10 +315,13 @@ struct TcDigits<float2> {
 
 // Pool layout of a tensor-core gate (bytes): int32 E_col[2D], then NDB digit
 // planes of B^T, each 2D rows of (2D + 8) fp16 (row j holds column j of B).
+// tab_key names the op whose group/offset tables the scratch holds (the
+// tables depend only on the op, so a CTA builds them once per pass when the
+// pass has one tensor-core gate); key is this op's identity in the pass.
 template <int K, class V>
 __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restrict__ dst,
                                          const unsigned char* __restrict__ pool, const OpDesc& op, int q,
-                                         unsigned char* __restrict__ scratch) {
+                                         unsigned char* __restrict__ scratch, int& tab_key, int key) {
     using TD = TcDigits<V>;
     constexpr bool kC128 = std::is_same<V, double2>::value;
     constexpr int ND = TD::kA;
@@ -338,33 +341,37 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
     uint32_t* offt = gbt + G;
     // pool column scales: complex128 int32 E_col; complex64 float 2^(E_col - 19)
 
-    int ss[K];
-    uint32_t bitv[K];
-#pragma unroll
-    for (int j = 0; j < K; ++j) {
-        ss[j] = op.tslot[j];
-        bitv[j] = 1u << op.tslot[j];
-    }
-#pragma unroll
-    for (int a = 1; a < K; ++a)
-#pragma unroll
-        for (int b = K - 1; b >= a; --b)
-            if (ss[b - 1] > ss[b]) { const int t = ss[b]; ss[b] = ss[b - 1]; ss[b - 1] = t; }
-    auto group_base = [&](uint32_t g) {
+    if (tab_key != key) {
+        int ss[K];
+        uint32_t bitv[K];
 #pragma unroll
         for (int j = 0; j < K; ++j) {
-            const uint32_t low = g & ((1u << ss[j]) - 1u);
-            g = ((g - low) << 1) | low;
+            ss[j] = op.tslot[j];
+            bitv[j] = 1u << op.tslot[j];
         }
-        return g;
-    };
-    auto offset_of = [&](int c) {
-        uint32_t o = 0;
 #pragma unroll
-        for (int j = 0; j < K; ++j)
-            if ((c >> j) & 1) o |= bitv[j];
-        return o;
-    };
+        for (int a = 1; a < K; ++a)
+#pragma unroll
+            for (int b = K - 1; b >= a; --b)
+                if (ss[b - 1] > ss[b]) { const int t = ss[b]; ss[b] = ss[b - 1]; ss[b - 1] = t; }
+        for (int g = threadIdx.x; g < G; g += blockDim.x) {
+            uint32_t v = (uint32_t)g;
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                const uint32_t low = v & ((1u << ss[j]) - 1u);
+                v = ((v - low) << 1) | low;
+            }
+            gbt[g] = v;
+        }
+        for (int c = threadIdx.x; c < D; c += blockDim.x) {
+            uint32_t o = 0;
+#pragma unroll
+            for (int j = 0; j < K; ++j)
+                if ((c >> j) & 1) o |= bitv[j];
+            offt[c] = o;
+        }
+        tab_key = key;
+    }
 
     // 1. digit planes of X. Plane column 2c + p holds part p (0 re, 1 im) of
     // input c. A work item is (group g, 4 consecutive inputs); consecutive
@@ -372,11 +379,7 @@ __device__ __forceinline__ void apply_tc(const V* __restrict__ src, V* __restric
     // whenever tile bit 0 is not a target.
     constexpr int CPI = 2;           // complex inputs per item
     constexpr int NCH = D / CPI;     // items per group
-    for (int g = threadIdx.x; g < G; g += blockDim.x) {
-        erow[g] = 0;
-        gbt[g] = group_base(g);
-    }
-    for (int c = threadIdx.x; c < D; c += blockDim.x) offt[c] = offset_of(c);
+    for (int g = threadIdx.x; g < G; g += blockDim.x) erow[g] = 0;
     __syncthreads();
     for (int it = threadIdx.x; it < G * NCH; it += blockDim.x) {
         const int g = it % G, ch = it / G;
@@ -677,16 +680,42 @@ __device__ __forceinline__ uint64_t tile_base(const PassDesc& d, uint64_t t) {
     return base | d.fixed_mask;
 }
 
-// Issue this thread's copies of tile t into the staging buffer.
+// A CTA's walk over tiles t0, t0 + stride, ...: the base of the next tile is
+// the current one plus the deposited stride, added with the carries skipping
+// every position outside `spread` (the bits tile numbers are spread over).
+struct TileWalk {
+    uint64_t spread, step, base, fixed;
+    __device__ __forceinline__ TileWalk(const PassDesc& d, uint64_t t0, uint64_t stride) {
+        uint64_t ins = 0;
+        for (int i = 0; i < d.nins; ++i) ins |= 1ULL << d.ins_pos[i];
+        spread = ~ins & (d.n >= 64 ? ~0ULL : ((1ULL << d.n) - 1ULL));
+        fixed = d.fixed_mask;
+        base = tile_base(d, t0);
+        step = tile_base(d, stride) & ~fixed;
+    }
+    __device__ __forceinline__ uint64_t after(uint64_t b) const {
+        return ((((b & spread) | ~spread) + step) & spread) | fixed;
+    }
+};
+
+// Issue this thread's copies of tile t into buf (its own slots: the same
+// L = threadIdx.x + i * blockDim.x as every load, conversion and store).
 template <class A>
-__device__ __forceinline__ void tile_prefetch(const typename A::store_t* __restrict__ state, const PassDesc& d,
-                                              const PassSmem<A>& sm, uint64_t t) {
+__device__ __forceinline__ void tile_prefetch_into(const typename A::store_t* __restrict__ state, const PassDesc& d,
+                                                   const PassSmem<A>& sm, uint64_t base,
+                                                   typename A::store_t* __restrict__ buf) {
     const int Q = 1 << d.q;
     const uint32_t lowmask = (1u << d.w) - 1u;
-    const uint64_t base = tile_base(d, t);
     for (int L = threadIdx.x; L < Q; L += blockDim.x)
-        cp_async_elem(sm.stage + L, state + base + sm.hoff[L >> d.w] + (L & lowmask));
+        cp_async_elem(buf + L, state + base + sm.hoff[L >> d.w] + (L & lowmask));
     cp_async_commit();
+}
+
+// ... into the staging buffer.
+template <class A>
+__device__ __forceinline__ void tile_prefetch(const typename A::store_t* __restrict__ state, const PassDesc& d,
+                                              const PassSmem<A>& sm, uint64_t base) {
+    tile_prefetch_into<A>(state, d, sm, base, sm.stage);
 }
 
 // Stage a pass's matrices and tile offsets into shared memory.
@@ -704,22 +733,26 @@ __device__ __forceinline__ void pass_setup(const PassSmem<A>& sm, const PassDesc
     __syncthreads();
 }
 
-// One tile of a pass: load (unless the caller already placed the tile in
-// bufA), apply the pass's gates in order, store.
+// One tile of a pass: load into b0 (unless the caller already placed the
+// tile there), apply the pass's gates in order, store. b1 is the other tile
+// buffer (dense gates ping-pong between the two). With d.prefetch == 2 every
+// op of the pass works in place on b0 (tensor-core digit gates, diagonal and
+// scalar ops), and b1 belongs to the caller.
 template <class A>
 __device__ __forceinline__ void pass_tile(typename A::store_t* __restrict__ state, const PassDesc& d,
-                                          const PassSmem<A>& sm, uint64_t t, bool loaded = false) {
+                                          const PassSmem<A>& sm, uint64_t base, int& tab_key, bool loaded = false,
+                                          typename A::comp_t* b0 = nullptr, typename A::comp_t* b1 = nullptr) {
     using C = typename A::comp_t;
     const int Q = 1 << d.q;
     const uint32_t lowmask = (1u << d.w) - 1u;
-    const uint64_t base = tile_base(d, t);
+    const bool inplace = d.prefetch == 2;
+    C* src = b0 ? b0 : sm.bufA;
+    C* dst = b1 ? b1 : sm.bufB;
     if (!loaded) {
         for (int L = threadIdx.x; L < Q; L += blockDim.x)
-            sm.bufA[L] = A::to_comp(state[base + sm.hoff[L >> d.w] + (L & lowmask)]);
+            src[L] = A::to_comp(state[base + sm.hoff[L >> d.w] + (L & lowmask)]);
         __syncthreads();
     }
-    C* src = sm.bufA;
-    C* dst = sm.bufB;
     for (int oi = 0; oi < d.nops; ++oi) {
         const OpDesc& op = d.ops[oi];
         if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
@@ -750,16 +783,21 @@ __device__ __forceinline__ void pass_tile(typename A::store_t* __restrict__ stat
         }
         if constexpr (A::kId == 4 || A::kId == 6) {
             if (op.tc) {
+                // the digit planes decouple the MMA reads from the tile, so
+                // the gate can also write its result over its input
                 const unsigned char* pool = reinterpret_cast<const unsigned char*>(sm.smat + op.mat_off);
+                C* out = inplace ? src : dst;
                 switch (op.k) {
-                    case 3: apply_tc<3, C>(src, dst, pool, op, d.q, sm.tcs); break;
-                    case 4: apply_tc<4, C>(src, dst, pool, op, d.q, sm.tcs); break;
-                    default: apply_tc<5, C>(src, dst, pool, op, d.q, sm.tcs); break;
+                    case 3: apply_tc<3, C>(src, out, pool, op, d.q, sm.tcs, tab_key, oi); break;
+                    case 4: apply_tc<4, C>(src, out, pool, op, d.q, sm.tcs, tab_key, oi); break;
+                    default: apply_tc<5, C>(src, out, pool, op, d.q, sm.tcs, tab_key, oi); break;
                 }
                 __syncthreads();
-                C* tmp = src;
-                src = dst;
-                dst = tmp;
+                if (!inplace) {
+                    C* tmp = src;
+                    src = dst;
+                    dst = tmp;
+                }
                 continue;
             }
         }
@@ -792,21 +830,50 @@ __global__ void __launch_bounds__(kThreads, pass_min_blocks(A::kId)) pass_kernel
     const PassSmem<A> sm(smem, d);
     pass_setup<A>(sm, d, mats);
     const uint64_t ntiles = 1ULL << (d.n - d.nins);
+    if ((uint64_t)blockIdx.x >= ntiles) return;
+    const TileWalk walk(d, blockIdx.x, gridDim.x);
+    int tab_key = -1;
     if (!d.prefetch) {
-        for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) pass_tile<A>(state, d, sm, t);
+        uint64_t base = walk.base;
+        for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x, base = walk.after(base))
+            pass_tile<A>(state, d, sm, base, tab_key);
         return;
+    }
+    if constexpr (std::is_same<typename A::comp_t, typename A::store_t>::value) {
+        if (d.prefetch == 2) {
+            // all ops in place: tile t + gridDim.x streams into the other tile
+            // buffer while tile t is computed; the buffers swap every tile
+            typename A::comp_t* cur = sm.bufA;
+            typename A::comp_t* nxt = sm.bufB;
+            uint64_t base = walk.base;
+            tile_prefetch_into<A>(state, d, sm, base, cur);
+            for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+                const uint64_t next = walk.after(base);
+                cp_async_wait_all();
+                if (t + gridDim.x < ntiles) tile_prefetch_into<A>(state, d, sm, next, nxt);
+                __syncthreads();
+                pass_tile<A>(state, d, sm, base, tab_key, true, cur, nxt);
+                typename A::comp_t* tmp = cur;
+                cur = nxt;
+                nxt = tmp;
+                base = next;
+            }
+            return;
+        }
     }
     // software pipeline: tile t + gridDim.x streams into the staging buffer
     // while tile t is computed
     const int Q = 1 << d.q;
-    uint64_t t = blockIdx.x;
-    if (t < ntiles) tile_prefetch<A>(state, d, sm, t);
-    for (; t < ntiles; t += gridDim.x) {
+    uint64_t base = walk.base;
+    tile_prefetch<A>(state, d, sm, base);
+    for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+        const uint64_t next = walk.after(base);
         cp_async_wait_all();
         for (int L = threadIdx.x; L < Q; L += blockDim.x) sm.bufA[L] = A::to_comp(sm.stage[L]);
-        if (t + gridDim.x < ntiles) tile_prefetch<A>(state, d, sm, t + gridDim.x);
+        if (t + gridDim.x < ntiles) tile_prefetch<A>(state, d, sm, next);
         __syncthreads();
-        pass_tile<A>(state, d, sm, t, true);
+        pass_tile<A>(state, d, sm, base, tab_key, true);
+        base = next;
     }
 }
 
@@ -819,6 +886,7 @@ __global__ void __launch_bounds__(kThreads, pass_min_blocks(A::kId)) batch_pass_
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ PassDesc sd;
     int cur = -1;
+    int tab_key = -1;
     // runs of 8 consecutive tiles, dealt round-robin to the CTAs: a CTA
     // re-stages an item's matrices at most once per run, and every CTA sees
     // a mix of cheap and expensive items
@@ -832,6 +900,7 @@ __global__ void __launch_bounds__(kThreads, pass_min_blocks(A::kId)) batch_pass_
             else hi = mid - 1;
         }
         if (lo != cur) {
+            tab_key = -1;
             __syncthreads();
             const uint32_t* srcw = reinterpret_cast<const uint32_t*>(&items[lo].desc);
             uint32_t* dstw = reinterpret_cast<uint32_t*>(&sd);
@@ -841,7 +910,7 @@ __global__ void __launch_bounds__(kThreads, pass_min_blocks(A::kId)) batch_pass_
             pass_setup<A>(PassSmem<A>(smem, sd), sd, reinterpret_cast<const typename A::mat_t*>(items[lo].mats));
         }
         pass_tile<A>(reinterpret_cast<typename A::store_t*>(items[lo].state), sd, PassSmem<A>(smem, sd),
-                     T - items[lo].tile_begin);
+                     tile_base(sd, T - items[lo].tile_begin), tab_key);
     }
 }
 
@@ -849,7 +918,7 @@ template <class A>
 size_t pass_smem_t(const PassDesc& d) {
     const size_t mat_bytes = ((size_t)d.mat_elems * sizeof(typename A::mat_t) + 15) & ~(size_t)15;
     return ((mat_bytes + 2 * (sizeof(typename A::comp_t) << d.q) + sizeof(uint64_t) * (1u << (d.q - d.w)) + 15) &
-            ~(size_t)15) + d.tc_bytes + (d.prefetch ? (sizeof(typename A::store_t) << d.q) : 0);
+            ~(size_t)15) + d.tc_bytes + (d.prefetch == 1 ? (sizeof(typename A::store_t) << d.q) : 0);
 }
 
 template <class A>

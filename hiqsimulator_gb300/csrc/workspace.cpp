@@ -227,10 +227,21 @@ std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t no
         }
         d.mat_elems = moff;
         d.tc_bytes = (uint32_t)((tcb + 15) & ~(size_t)15);
-        // stream the next tile in while computing this one, unless the staging
-        // buffer would cost a resident CTA per SM (228 KB per SM, 1 KB
-        // reserved per CTA, at most 227 KB per CTA)
-        {
+        // stream the next tile in while computing this one: into the second
+        // tile buffer when every op works in place on raw state elements,
+        // else into a staging buffer unless that costs a resident CTA per SM
+        // (228 KB per SM, 1 KB reserved per CTA, at most 227 KB per CTA)
+        bool inplace = true, has_tc_op = false;
+        for (int o = 0; o < d.nops; ++o) {
+            const OpDesc& od = d.ops[o];
+            has_tc_op = has_tc_op || od.tc;
+            inplace = inplace && (od.k == 0 || od.diag || (od.tc && arith != kArithTF32));
+        }
+        const bool raw = arith == kArithF64 || arith == kArithF32 || arith == kArithTF32 || arith == kArithTC64 ||
+                         (arith == kArithTC && has_tc_op);
+        if (raw && inplace && d.nops > 0) {
+            d.prefetch = 2;
+        } else {
             const int regc = pass_reg_ctas(arith, d);
             auto ctas = [&](size_t sm) { return std::min<size_t>((size_t)regc, 233472 / (sm + 1024)); };
             d.prefetch = 0;
