@@ -122,6 +122,11 @@ struct ArithF64 {
     __device__ __forceinline__ static comp_t mul(const mat_t m, const comp_t v) {
         return make_double2(fma(m.x, v.x, -m.y * v.y), fma(m.x, v.y, m.y * v.x));
     }
+    // element-wise chains (runs of diagonal and scalar gates) work on comp_t itself
+    using elem_t = comp_t;
+    __device__ __forceinline__ static elem_t elem_load(const comp_t v) { return v; }
+    __device__ __forceinline__ static comp_t elem_store(const elem_t v) { return v; }
+    __device__ __forceinline__ static elem_t elem_mul(const mat_t m, const elem_t v) { return mul(m, v); }
 };
 
 struct ArithDF {
@@ -155,6 +160,11 @@ struct ArithDF {
         mac(a, m, v);
         return finish(a);
     }
+    // element-wise chains (runs of diagonal and scalar gates) work on comp_t itself
+    using elem_t = comp_t;
+    __device__ __forceinline__ static elem_t elem_load(const comp_t v) { return v; }
+    __device__ __forceinline__ static comp_t elem_store(const elem_t v) { return v; }
+    __device__ __forceinline__ static elem_t elem_mul(const mat_t m, const elem_t v) { return mul(m, v); }
 };
 
 struct ArithF32 {
@@ -176,6 +186,11 @@ struct ArithF32 {
     __device__ __forceinline__ static comp_t mul(const mat_t m, const comp_t v) {
         return make_float2(fmaf(m.x, v.x, -m.y * v.y), fmaf(m.x, v.y, m.y * v.x));
     }
+    // element-wise chains (runs of diagonal and scalar gates) work on comp_t itself
+    using elem_t = comp_t;
+    __device__ __forceinline__ static elem_t elem_load(const comp_t v) { return v; }
+    __device__ __forceinline__ static comp_t elem_store(const elem_t v) { return v; }
+    __device__ __forceinline__ static elem_t elem_mul(const mat_t m, const elem_t v) { return mul(m, v); }
 };
 
 // complex64 passes that also run 3xTF32 tensor-core gates: the same FP32
@@ -209,6 +224,12 @@ struct ArithDFRaw {
     __device__ __forceinline__ static comp_t mul(const mat_t m, const comp_t v) {
         return ArithDF::from_comp(ArithDF::mul(m, ArithDF::to_comp(v)));
     }
+    // a run of diagonal and scalar gates splits each amplitude once, multiplies
+    // in double-float, and re-assembles once
+    using elem_t = float4;
+    __device__ __forceinline__ static elem_t elem_load(const comp_t v) { return ArithDF::to_comp(v); }
+    __device__ __forceinline__ static comp_t elem_store(const elem_t v) { return ArithDF::from_comp(v); }
+    __device__ __forceinline__ static elem_t elem_mul(const mat_t m, const elem_t v) { return ArithDF::mul(m, v); }
 };
 
 // -------------------------------------------------- |a|^2 accumulation policies

@@ -15,6 +15,7 @@ namespace hqs {
 constexpr int kMaxOpsPerPass = 24;
 constexpr int kMaxTileBits = 12;
 constexpr int kMaxK = 5;
+constexpr uint8_t kOuterSlot = 0x80;
 
 // Arithmetic used by the apply kernels.
 enum Arith : int32_t {
@@ -47,7 +48,8 @@ struct OpDesc {
     uint32_t ctrl_local;  // tile-local bits that must all be 1
     uint32_t mat_off;     // offset (elements) of this op's matrix in the pass pool
     uint64_t ctrl_outer;  // state bits outside the tile that must all be 1
-    uint8_t tslot[kMaxK]; // tile-local bit of matrix bit j
+    uint8_t tslot[kMaxK]; // tile-local bit of matrix bit j; diagonal gates may have targets
+                          // outside the tile: kOuterSlot | state position
     uint8_t tc;           // 1: dense gate applied on the tensor cores (digit planes in the pool)
     uint8_t pad[2];
 };

@@ -95,14 +95,49 @@ cudaError_t finish_reduce(int nparts, ReduceScratch& rs, cudaStream_t s, double*
 
 // ---------------------------------------------------------------- fused pass
 
+// Diagonal gate in place. A target inside the tile reads its tile-local bit;
+// a target outside it (tslot = kOuterSlot | state position) reads the tile
+// base's bit, the same for every amplitude of the tile.
 template <class A>
 __device__ __forceinline__ void apply_diag(typename A::comp_t* buf, const typename A::mat_t* diag, const OpDesc& op,
-                                           int Q) {
+                                           int Q, uint64_t base) {
+    int rout = 0;
+    for (int j = 0; j < op.k; ++j)
+        if (op.tslot[j] & kOuterSlot) rout |= (int)((base >> (op.tslot[j] & 63)) & 1ULL) << j;
     for (int L = threadIdx.x; L < Q; L += blockDim.x) {
         if ((L & op.ctrl_local) != op.ctrl_local) continue;
-        int r = 0;
-        for (int j = 0; j < op.k; ++j) r |= ((L >> op.tslot[j]) & 1) << j;
+        int r = rout;
+        for (int j = 0; j < op.k; ++j)
+            if (!(op.tslot[j] & kOuterSlot)) r |= ((L >> op.tslot[j]) & 1) << j;
         buf[L] = A::mul(diag[r], buf[L]);
+    }
+}
+
+// A run of consecutive diagonal and scalar gates [o0, o1) in place: every
+// amplitude is loaded once, multiplied by each gate's entry (gates whose
+// outer controls this tile fails are skipped) and stored once.
+template <class A>
+__device__ __forceinline__ void apply_elementwise_run(typename A::comp_t* buf, const typename A::mat_t* pool,
+                                                      const PassDesc& d, int o0, int o1, int Q, uint64_t base) {
+    for (int L = threadIdx.x; L < Q; L += blockDim.x) {
+        typename A::elem_t x = A::elem_load(buf[L]);
+        for (int o = o0; o < o1; ++o) {
+            const OpDesc& op = d.ops[o];
+            if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
+            if (op.k == 0) {
+                x = A::elem_mul(pool[op.mat_off], x);
+                continue;
+            }
+            if ((L & op.ctrl_local) != op.ctrl_local) continue;
+            int r = 0;
+            for (int j = 0; j < op.k; ++j) {
+                const int sl = op.tslot[j];
+                const uint64_t bit = (sl & kOuterSlot) ? (base >> (sl & 63)) : ((uint64_t)L >> sl);
+                r |= (int)(bit & 1ULL) << j;
+            }
+            x = A::elem_mul(pool[op.mat_off + r], x);
+        }
+        buf[L] = A::elem_store(x);
     }
 }
 
@@ -755,17 +790,17 @@ __device__ __forceinline__ void pass_tile(typename A::store_t* __restrict__ stat
     }
     for (int oi = 0; oi < d.nops; ++oi) {
         const OpDesc& op = d.ops[oi];
+        if (op.k == 0 || op.diag) {
+            // consecutive diagonal / scalar gates act element by element:
+            // one sweep over the tile for the whole run, no barrier between them
+            int end = oi + 1;
+            while (end < d.nops && (d.ops[end].k == 0 || d.ops[end].diag)) ++end;
+            apply_elementwise_run<A>(src, sm.smat, d, oi, end, Q, base);
+            __syncthreads();
+            oi = end - 1;
+            continue;
+        }
         if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
-        if (op.k == 0) {
-            apply_scalar<A>(src, sm.smat[op.mat_off], Q);
-            __syncthreads();
-            continue;
-        }
-        if (op.diag) {
-            apply_diag<A>(src, sm.smat + op.mat_off, op, Q);
-            __syncthreads();
-            continue;
-        }
         if constexpr (A::kId == 5) {
             if (op.tc) {
                 const float4* frag = reinterpret_cast<const float4*>(sm.smat + op.mat_off);

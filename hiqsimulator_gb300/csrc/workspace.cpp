@@ -145,8 +145,11 @@ std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t no
         if (op_first) op_first->push_back(i);
         while (j < nops && (int)(j - i) < max_ops) {
             const GateOp& op = ops[j];
+            // a diagonal gate needs none of its targets in the tile (the tile
+            // base supplies the bits of those outside it)
             uint64_t tm = 0;
-            for (int t = 0; t < op.k; ++t) tm |= 1ULL << op.pos[t];
+            if (!op.diag)
+                for (int t = 0; t < op.k; ++t) tm |= 1ULL << op.pos[t];
             const uint64_t ns = tset | tm;
             const size_t ob = pool_elems(arith, op, tc_candidate(arith, op)) * melem;
             if (j > i && (popc64(ns) + 4 > max_tile_bits || mbytes + ob > mat_budget)) break;
@@ -221,7 +224,9 @@ std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t no
             for (int b = 0; b < n; ++b)
                 if (((op.ctrl_mask & tile) >> b) & 1ULL) cl |= 1u << slot[b];
             od.ctrl_local = cl;
-            for (int t = 0; t < op.k; ++t) od.tslot[t] = (uint8_t)slot[op.pos[t]];
+            for (int t = 0; t < op.k; ++t)
+                od.tslot[t] = ((tile >> op.pos[t]) & 1ULL) ? (uint8_t)slot[op.pos[t]]
+                                                             : (uint8_t)(kOuterSlot | op.pos[t]);
             od.mat_off = moff;
             moff += (uint32_t)pool_elems(arith, op, od.tc != 0);
         }
