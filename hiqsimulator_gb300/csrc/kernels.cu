@@ -95,24 +95,6 @@ cudaError_t finish_reduce(int nparts, ReduceScratch& rs, cudaStream_t s, double*
 
 // ---------------------------------------------------------------- fused pass
 
-// Diagonal gate in place. A target inside the tile reads its tile-local bit;
-// a target outside it (tslot = kOuterSlot | state position) reads the tile
-// base's bit, the same for every amplitude of the tile.
-template <class A>
-__device__ __forceinline__ void apply_diag(typename A::comp_t* buf, const typename A::mat_t* diag, const OpDesc& op,
-                                           int Q, uint64_t base) {
-    int rout = 0;
-    for (int j = 0; j < op.k; ++j)
-        if (op.tslot[j] & kOuterSlot) rout |= (int)((base >> (op.tslot[j] & 63)) & 1ULL) << j;
-    for (int L = threadIdx.x; L < Q; L += blockDim.x) {
-        if ((L & op.ctrl_local) != op.ctrl_local) continue;
-        int r = rout;
-        for (int j = 0; j < op.k; ++j)
-            if (!(op.tslot[j] & kOuterSlot)) r |= ((L >> op.tslot[j]) & 1) << j;
-        buf[L] = A::mul(diag[r], buf[L]);
-    }
-}
-
 // A run of consecutive diagonal and scalar gates [o0, o1) in place: every
 // amplitude is loaded once, multiplied by each gate's entry (gates whose
 // outer controls this tile fails are skipped) and stored once.
@@ -139,11 +121,6 @@ __device__ __forceinline__ void apply_elementwise_run(typename A::comp_t* buf, c
         }
         buf[L] = A::elem_store(x);
     }
-}
-
-template <class A>
-__device__ __forceinline__ void apply_scalar(typename A::comp_t* buf, const typename A::mat_t m, int Q) {
-    for (int L = threadIdx.x; L < Q; L += blockDim.x) buf[L] = A::mul(m, buf[L]);
 }
 
 // Dense k-qubit op, tile src -> tile dst. The matrix is stored transposed

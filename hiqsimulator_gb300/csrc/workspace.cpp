@@ -129,10 +129,126 @@ static size_t pool_elems(int arith, const GateOp& op, bool tc) {
     return op.m.size();
 }
 
+// Pass over ops [i, j): tile, op descriptors, prefetch mode, sweep bytes
+// (pool_off is set by the caller).
+static PassPlan build_pass(int n, int arith, const GateOp* ops, size_t i, size_t j, int max_tile_bits) {
+    const size_t melem = Workspace::mat_elem_bytes(arith);
+    const size_t store = arith_is_c64(arith) ? 8 : 16;
+    uint64_t tset = 0;
+    for (size_t o = i; o < j; ++o)
+        if (!ops[o].diag)
+            for (int t = 0; t < ops[o].k; ++t) tset |= 1ULL << ops[o].pos[t];
+    PassPlan pl;
+    PassDesc& d = pl.desc;
+    std::memset(&d, 0, sizeof(d));
+    // tile: the pass's targets plus at least 4 low positions, 2^10 amplitudes
+    // at least (enough index groups for every thread), at most 2^max_tile_bits
+    // complex128 digit-plane passes use 2^9-amplitude tiles (16 index
+    // groups for a 5-qubit gate) so that three CTAs fit on an SM next to
+    // the gate's digit planes; 3xTF32 passes 2^11 (64 groups: every warp
+    // gets a task of four n-tiles)
+    bool has_tc = false;
+    for (size_t o = i; o < j; ++o) has_tc = has_tc || tc_candidate(arith, ops[o]);
+    const int base_q = !has_tc ? 10 : arith == kArithTF32 ? 11 : arith == kArithTC ? 9 : 10;
+    int q = std::min(n, std::max(popc64(tset), std::min(max_tile_bits, std::max(popc64(tset) + 4, base_q))));
+    // keep the pass within one CTA's shared memory: shrink the tile (not
+    // below the targets), then give up tensor-core gates if still too big
+    bool allow_tc = true;
+    auto smem_estimate = [&](int qq, bool tcok) {
+        size_t mat = 0, tcb = 0;
+        for (size_t o = i; o < j; ++o) {
+            const bool tc = tcok && tc_candidate(arith, ops[o]) && qq >= ops[o].k + 4;
+            mat += pool_elems(arith, ops[o], tc) * melem + (tc ? 8 : 0);
+            if (tc) tcb = std::max(tcb, tc_scratch_bytes(arith, qq, ops[o].k));
+        }
+        return mat + 2 * (store << qq) + 8 * ((size_t)1 << qq) + 32 + tcb;
+    };
+    const size_t smem_budget = 200 * 1024;
+    while (smem_estimate(q, allow_tc) > smem_budget && q > std::max(popc64(tset), std::min(n, 10))) --q;
+    if (smem_estimate(q, allow_tc) > smem_budget) allow_tc = false;
+    uint64_t tile = tset;
+    for (int b = 0; b < n && popc64(tile) < q; ++b) tile |= 1ULL << b;
+    int slot[64];
+    int c = 0;
+    for (int b = 0; b < n; ++b)
+        if ((tile >> b) & 1ULL) {
+            slot[b] = c;
+            d.tile_pos[c++] = (uint8_t)b;
+        }
+    d.n = n;
+    d.q = q;
+    d.w = 0;
+    while (d.w < q && d.tile_pos[d.w] == d.w) ++d.w;
+    uint64_t fixed = ~0ULL;
+    for (size_t o = i; o < j; ++o) fixed &= ops[o].ctrl_mask & ~tile;
+    if (j == i) fixed = 0;
+    d.fixed_mask = fixed;
+    const uint64_t ins = tile | fixed;
+    d.nins = 0;
+    for (int b = 0; b < 64; ++b)
+        if ((ins >> b) & 1ULL) d.ins_pos[d.nins++] = (uint8_t)b;
+    d.nops = (int)(j - i);
+    uint32_t moff = 0;
+    size_t tcb = 0;
+    for (size_t o = i; o < j; ++o) {
+        const GateOp& op = ops[o];
+        OpDesc& od = d.ops[o - i];
+        od.k = op.k;
+        od.diag = op.diag ? 1 : 0;
+        // tensor-core gates need at least 16 index groups per tile
+        od.tc = (allow_tc && tc_candidate(arith, op) && q >= op.k + 4) ? 1 : 0;
+        // 3xTF32 fragments are read as float4: 16-byte aligned in the pool
+        if (od.tc && arith == kArithTF32) moff = (moff + 1) & ~1u;
+        if (od.tc) tcb = std::max(tcb, tc_scratch_bytes(arith, q, op.k));
+        od.ctrl_outer = op.ctrl_mask & ~tile;
+        uint32_t cl = 0;
+        for (int b = 0; b < n; ++b)
+            if (((op.ctrl_mask & tile) >> b) & 1ULL) cl |= 1u << slot[b];
+        od.ctrl_local = cl;
+        for (int t = 0; t < op.k; ++t)
+            od.tslot[t] = ((tile >> op.pos[t]) & 1ULL) ? (uint8_t)slot[op.pos[t]]
+                                                         : (uint8_t)(kOuterSlot | op.pos[t]);
+        od.mat_off = moff;
+        moff += (uint32_t)pool_elems(arith, op, od.tc != 0);
+    }
+    d.mat_elems = moff;
+    d.tc_bytes = (uint32_t)((tcb + 15) & ~(size_t)15);
+    // stream the next tile in while computing this one: into the second
+    // tile buffer when every op works in place on raw state elements,
+    // else into a staging buffer unless that costs a resident CTA per SM
+    // (228 KB per SM, 1 KB reserved per CTA, at most 227 KB per CTA)
+    bool inplace = true, has_tc_op = false;
+    for (int o = 0; o < d.nops; ++o) {
+        const OpDesc& od = d.ops[o];
+        has_tc_op = has_tc_op || od.tc;
+        inplace = inplace && (od.k == 0 || od.diag || (od.tc && arith != kArithTF32));
+    }
+    const bool raw = arith == kArithF64 || arith == kArithF32 || arith == kArithTF32 || arith == kArithTC64 ||
+                     (arith == kArithTC && has_tc_op);
+    if (raw && inplace && d.nops > 0) {
+        d.prefetch = 2;
+    } else {
+        const int regc = pass_reg_ctas(arith, d);
+        auto ctas = [&](size_t sm) { return std::min<size_t>((size_t)regc, 233472 / (sm + 1024)); };
+        d.prefetch = 0;
+        const size_t s0 = pass_smem_bytes(arith, d);
+        d.prefetch = 1;
+        const size_t s1 = pass_smem_bytes(arith, d);
+        d.prefetch = (s1 <= 232448 && ctas(s1) >= ctas(s0)) ? 1 : 0;
+    }
+    pl.bytes = 2ULL * (1ULL << (n - popc64(fixed))) * store;
+    return pl;
+}
+
+// Resident CTAs per SM of a pass: its kernel's register budget and its
+// shared memory (228 KB per SM, 1 KB reserved per CTA).
+static int pass_ctas(int arith, const PassDesc& d) {
+    return std::min(pass_reg_ctas(arith, d), (int)(233472 / (pass_smem_bytes(arith, d) + 1024)));
+}
+
 std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t nops, int max_tile_bits, int max_ops,
                                   std::vector<size_t>* op_first, size_t max_passes) {
     const size_t melem = Workspace::mat_elem_bytes(arith);
-    const size_t store = arith_is_c64(arith) ? 8 : 16;
     // staged matrices per pass; 3xTF32 passes take two 5-qubit gates
     const size_t mat_budget = (arith == kArithTF32 ? 72 : 64) * 1024;
     max_tile_bits = std::max(5, std::min(max_tile_bits, kMaxTileBits));
@@ -157,107 +273,18 @@ std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t no
             mbytes += ob;
             ++j;
         }
-        PassPlan pl;
-        PassDesc& d = pl.desc;
-        std::memset(&d, 0, sizeof(d));
-        // tile: the pass's targets plus at least 4 low positions, 2^10 amplitudes
-        // at least (enough index groups for every thread), at most 2^max_tile_bits
-        // complex128 digit-plane passes use 2^9-amplitude tiles (16 index
-        // groups for a 5-qubit gate) so that three CTAs fit on an SM next to
-        // the gate's digit planes; 3xTF32 passes 2^11 (64 groups: every warp
-        // gets a task of four n-tiles)
-        bool has_tc = false;
-        for (size_t o = i; o < j; ++o) has_tc = has_tc || tc_candidate(arith, ops[o]);
-        const int base_q = !has_tc ? 10 : arith == kArithTF32 ? 11 : arith == kArithTC ? 9 : 10;
-        int q = std::min(n, std::max(popc64(tset), std::min(max_tile_bits, std::max(popc64(tset) + 4, base_q))));
-        // keep the pass within one CTA's shared memory: shrink the tile (not
-        // below the targets), then give up tensor-core gates if still too big
-        bool allow_tc = true;
-        auto smem_estimate = [&](int qq, bool tcok) {
-            size_t mat = 0, tcb = 0;
-            for (size_t o = i; o < j; ++o) {
-                const bool tc = tcok && tc_candidate(arith, ops[o]) && qq >= ops[o].k + 4;
-                mat += pool_elems(arith, ops[o], tc) * melem + (tc ? 8 : 0);
-                if (tc) tcb = std::max(tcb, tc_scratch_bytes(arith, qq, ops[o].k));
+        PassPlan pl = build_pass(n, arith, ops, i, j, max_tile_bits);
+        // leave out trailing ops whose matrices would cost a resident CTA per
+        // SM: the pass then runs at the occupancy of its first op
+        if (j - i > 1) {
+            const int best = pass_ctas(arith, build_pass(n, arith, ops, i, i + 1, max_tile_bits).desc);
+            while (j - i > 1 && pass_ctas(arith, pl.desc) < best) {
+                --j;
+                pl = build_pass(n, arith, ops, i, j, max_tile_bits);
             }
-            return mat + 2 * (store << qq) + 8 * ((size_t)1 << qq) + 32 + tcb;
-        };
-        const size_t smem_budget = 200 * 1024;
-        while (smem_estimate(q, allow_tc) > smem_budget && q > std::max(popc64(tset), std::min(n, 10))) --q;
-        if (smem_estimate(q, allow_tc) > smem_budget) allow_tc = false;
-        uint64_t tile = tset;
-        for (int b = 0; b < n && popc64(tile) < q; ++b) tile |= 1ULL << b;
-        int slot[64];
-        int c = 0;
-        for (int b = 0; b < n; ++b)
-            if ((tile >> b) & 1ULL) {
-                slot[b] = c;
-                d.tile_pos[c++] = (uint8_t)b;
-            }
-        d.n = n;
-        d.q = q;
-        d.w = 0;
-        while (d.w < q && d.tile_pos[d.w] == d.w) ++d.w;
-        uint64_t fixed = ~0ULL;
-        for (size_t o = i; o < j; ++o) fixed &= ops[o].ctrl_mask & ~tile;
-        if (j == i) fixed = 0;
-        d.fixed_mask = fixed;
-        const uint64_t ins = tile | fixed;
-        d.nins = 0;
-        for (int b = 0; b < 64; ++b)
-            if ((ins >> b) & 1ULL) d.ins_pos[d.nins++] = (uint8_t)b;
-        d.nops = (int)(j - i);
-        uint32_t moff = 0;
-        size_t tcb = 0;
-        for (size_t o = i; o < j; ++o) {
-            const GateOp& op = ops[o];
-            OpDesc& od = d.ops[o - i];
-            od.k = op.k;
-            od.diag = op.diag ? 1 : 0;
-            // tensor-core gates need at least 16 index groups per tile
-            od.tc = (allow_tc && tc_candidate(arith, op) && q >= op.k + 4) ? 1 : 0;
-            // 3xTF32 fragments are read as float4: 16-byte aligned in the pool
-            if (od.tc && arith == kArithTF32) moff = (moff + 1) & ~1u;
-            if (od.tc) tcb = std::max(tcb, tc_scratch_bytes(arith, q, op.k));
-            od.ctrl_outer = op.ctrl_mask & ~tile;
-            uint32_t cl = 0;
-            for (int b = 0; b < n; ++b)
-                if (((op.ctrl_mask & tile) >> b) & 1ULL) cl |= 1u << slot[b];
-            od.ctrl_local = cl;
-            for (int t = 0; t < op.k; ++t)
-                od.tslot[t] = ((tile >> op.pos[t]) & 1ULL) ? (uint8_t)slot[op.pos[t]]
-                                                             : (uint8_t)(kOuterSlot | op.pos[t]);
-            od.mat_off = moff;
-            moff += (uint32_t)pool_elems(arith, op, od.tc != 0);
-        }
-        d.mat_elems = moff;
-        d.tc_bytes = (uint32_t)((tcb + 15) & ~(size_t)15);
-        // stream the next tile in while computing this one: into the second
-        // tile buffer when every op works in place on raw state elements,
-        // else into a staging buffer unless that costs a resident CTA per SM
-        // (228 KB per SM, 1 KB reserved per CTA, at most 227 KB per CTA)
-        bool inplace = true, has_tc_op = false;
-        for (int o = 0; o < d.nops; ++o) {
-            const OpDesc& od = d.ops[o];
-            has_tc_op = has_tc_op || od.tc;
-            inplace = inplace && (od.k == 0 || od.diag || (od.tc && arith != kArithTF32));
-        }
-        const bool raw = arith == kArithF64 || arith == kArithF32 || arith == kArithTF32 || arith == kArithTC64 ||
-                         (arith == kArithTC && has_tc_op);
-        if (raw && inplace && d.nops > 0) {
-            d.prefetch = 2;
-        } else {
-            const int regc = pass_reg_ctas(arith, d);
-            auto ctas = [&](size_t sm) { return std::min<size_t>((size_t)regc, 233472 / (sm + 1024)); };
-            d.prefetch = 0;
-            const size_t s0 = pass_smem_bytes(arith, d);
-            d.prefetch = 1;
-            const size_t s1 = pass_smem_bytes(arith, d);
-            d.prefetch = (s1 <= 232448 && ctas(s1) >= ctas(s0)) ? 1 : 0;
         }
         pl.pool_off = pool_off;
-        pool_off += ((size_t)moff * melem + 255) & ~(size_t)255;
-        pl.bytes = 2ULL * (1ULL << (n - popc64(fixed))) * store;
+        pool_off += ((size_t)pl.desc.mat_elems * melem + 255) & ~(size_t)255;
         plans.push_back(pl);
         i = j;
     }
