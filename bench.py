@@ -237,6 +237,68 @@ def capacity_report():
     return out
 
 
+def table_report(cmds30, ref_bytes30):
+    """Rows of the reference-against-GPU table. 20 qubits (random circuit,
+    20 layers; fusion off and greedy k <= 4): the oracle port of the
+    reference's algorithm on every host core, the GPU with one launch per
+    fused gate (the reference's one sweep per run(), no pass fusion), and the
+    GPU engine as shipped, with the max-abs error against the oracle.
+    30 qubits (the benchmark workload): the GPU with one launch per fused gate."""
+    import hiqsimulator_gb300 as hqs
+    from hiqsimulator_gb300 import circuits
+    from oracle.engine import OracleSimulator
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    out = {"host_threads": int(os.environ["OMP_NUM_THREADS"])}
+    n = 20
+    qs = list(range(n))
+    gates = circuits.random_circuit_20q(seed=1234, n=n, layers=20)
+    for mode, cmds in (("fusion_off", circuits.fusion_off_stream(gates)),
+                       ("greedy_k4", circuits.greedy_stream(gates, qs, 4))):
+        row = {}
+        ref = OracleSimulator(1234, n, 4)
+        ref.allocate_qureg(qs, 0)
+        t0 = time.perf_counter()
+        circuits.replay(ref, cmds)
+        ref.run()
+        row["cpu_oracle_ms"] = (time.perf_counter() - t0) * 1e3
+        for label, limits in (("gpu_one_fused_gate_per_launch_ms", dict(max_ops=1, defer=1)), ("gpu_ms", {})):
+            sim = hqs.SimulatorMPI(1234, n, 4, "c128")
+            if limits:
+                sim.set_pass_limits(**limits)
+            sim.allocate_qureg(qs, 0)
+            circuits.replay(sim, cmds)  # warm-up
+            sim.synchronize()
+            del sim
+            sim = hqs.SimulatorMPI(1234, n, 4, "c128")
+            if limits:
+                sim.set_pass_limits(**limits)
+            sim.allocate_qureg(qs, 0)
+            sim.synchronize()
+            sim.timer_start()
+            circuits.replay(sim, cmds)
+            sim.run()
+            row[label] = sim.timer_stop()
+            if not limits:
+                _, vec = sim.cheat_local_numpy()
+                row["max_abs_error_vs_oracle"] = float(np.max(np.abs(vec - ref.vec)))
+            del sim
+        out["random_20q_" + mode] = row
+        log("table 20q %s: cpu %.0f ms, gpu one fused gate per launch %.1f ms, gpu %.1f ms, err %.1e" % (
+            mode, row["cpu_oracle_ms"], row["gpu_one_fused_gate_per_launch_ms"], row["gpu_ms"], row["max_abs_error_vs_oracle"]))
+    sim = hqs.SimulatorMPI(SEED, N_QUBITS, CLUSTER, "c128")
+    sim.set_pass_limits(max_ops=1, defer=1)
+    sim.allocate_qureg(list(range(N_QUBITS)), 0)
+    sim.synchronize()
+    sim.timer_start()
+    circuits.replay(sim, cmds30)
+    sim.run()
+    ms = sim.timer_stop()
+    del sim
+    out["headline_one_fused_gate_per_launch"] = {"ms": ms, "GBs": ref_bytes30 / (ms / 1e3) / 1e9}
+    log("table %dq one fused gate per launch: %.0f ms, %.1f GB/s" % (N_QUBITS, ms, ref_bytes30 / (ms / 1e3) / 1e9))
+    return out
+
+
 def serving_report(args):
     """Serving of many small circuits: Poisson arrivals of circuits with
     n ~ U{10..22}, depth ~ U{10..60} random layers; batched continuous
@@ -429,6 +491,7 @@ def run_ours(args, dist):
     serv = serving_report(args) if (dist.rank == 0 and args.serve > 0) else None
     prec = precision_report() if (dist.rank == 0 and not args.no_precision) else None
     cap = capacity_report() if (dist.rank == 0 and args.capacity) else None
+    table = table_report(cmds, pass_ref_bytes) if (dist.rank == 0 and args.table) else None
 
     if dist.rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.ws, "steps": args.steps,
@@ -442,7 +505,7 @@ def run_ours(args, dist):
                            "state_bytes": 16 << N_QUBITS, "l2": "inputs larger than L2 (%d MiB state)" % ((16 << N_QUBITS) >> 20),
                            "parallelism": "replicas" if dist.ws > 1 else "single GPU"},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk, "serving": serv, "precision": prec, "capacity": cap}
+                "clocks": clk, "serving": serv, "precision": prec, "capacity": cap, "table": table}
         print(json.dumps(line), flush=True)
     return 0
 
@@ -463,6 +526,7 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=32, help="resident circuits at most while serving")
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--capacity", action="store_true", help="also run the 33q c128 / 34q c64 capacity states")
+    ap.add_argument("--table", action="store_true", help="also time the reference-against-GPU table rows")
     args = ap.parse_args()
     global N_QUBITS
     N_QUBITS = args.qubits
