@@ -491,6 +491,14 @@ double Engine::get_expectation_value(const std::vector<PauliTerm>& terms, const 
     pauli_masks(terms, ids, xm, ym, zm);
     if (terms.empty()) return 0.0;
     const size_t T = terms.size();
+    if (T == 1 && xm[0] == 0) {
+        // one Z string: <psi|Z..Z|psi> is real, Re(c <.>) = Re(c) <.>
+        double out = 0.0;
+        cuda_check(reduce_pauli_expectation(arith_, state_, n(), 1, nullptr, nullptr, nullptr, nullptr, ws_.reduce(),
+                                            ws_.stream(), &out, true, zm[0]),
+                   "reduce_pauli_expectation");
+        return terms[0].coef.real() * out;
+    }
     std::vector<unsigned char> blob(T * (3 * 8 + 16));
     std::memcpy(blob.data(), xm.data(), T * 8);
     std::memcpy(blob.data() + T * 8, ym.data(), T * 8);

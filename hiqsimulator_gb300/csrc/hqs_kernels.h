@@ -16,7 +16,7 @@ struct ReduceScratch {
     double* d_result = nullptr;    // 4 doubles
     double* h_result = nullptr;    // pinned, 4 doubles
 };
-constexpr int kMaxPartials = 1024;
+constexpr int kMaxPartials = 2048;
 
 int device_sm_count();
 
@@ -53,9 +53,12 @@ cudaError_t reduce_entropy(int arith, const void* state, int n, ReduceScratch& r
 // nblocks partial sums of |a|^2 over contiguous blocks, written to d_out (device).
 cudaError_t block_sums(int arith, const void* state, int n, uint64_t nblocks, double* d_out, cudaStream_t s);
 // Pauli-sum expectation: sum_t Re(c_t <psi|P_t|psi>); masks/coefs in device memory.
+// With zonly (one term, no X or Y) the device masks are not read: out is the
+// signed norm sum_i (-1)^popcount(i & zmask0) |a_i|^2, to be scaled by Re(c).
 cudaError_t reduce_pauli_expectation(int arith, const void* state, int n, int nterms, const uint64_t* d_xm,
                                      const uint64_t* d_ym, const uint64_t* d_zm, const double* d_coef,
-                                     ReduceScratch& rs, cudaStream_t s, double* out);
+                                     ReduceScratch& rs, cudaStream_t s, double* out, bool zonly = false,
+                                     uint64_t zmask0 = 0);
 
 // out = sum_t c_t P_t in (out-of-place; out and in must not alias). d_coef: per
 // term the pair (c_t i^{|Y_t|}, -c_t i^{|Y_t|}) in the arithmetic's matrix format.

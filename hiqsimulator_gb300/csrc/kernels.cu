@@ -73,9 +73,11 @@ __global__ void finish_partials(const double* __restrict__ partials, int nparts,
     }
 }
 
+// Reductions stream the state: 8 CTAs per SM keep enough loads in flight to
+// cover HBM latency.
 int reduce_grid(uint64_t work) {
     const uint64_t want = (work + kThreads - 1) / kThreads;
-    int g = device_sm_count() * 4;
+    int g = device_sm_count() * 8;
     if ((uint64_t)g > want) g = (int)std::max<uint64_t>(want, 1);
     return std::min(g, kMaxPartials);
 }
@@ -982,12 +984,18 @@ __global__ void __launch_bounds__(kThreads) probability_kernel(const S* __restri
                                                                double* __restrict__ partials) {
     __shared__ double red[32];
     NA acc;
-    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < count;
-         j += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t i = j;
-        for (int b = 0; b < m.npos; ++b) i = insert_zero(i, m.pos[b]);
-        acc.add(state[i | m.val]);
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    auto index = [&](uint64_t j) {
+        for (int b = 0; b < m.npos; ++b) j = insert_zero(j, m.pos[b]);
+        return j | m.val;
+    };
+    uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    for (; j + stride < count; j += 2 * stride) {  // two amplitudes in flight per thread
+        const S a0 = state[index(j)], a1 = state[index(j + stride)];
+        acc.add(a0);
+        acc.add(a1);
     }
+    if (j < count) acc.add(state[index(j)]);
     double v[1] = {acc.value()};
     block_sum<1>(v, red);
     if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
@@ -1071,6 +1079,58 @@ __device__ __forceinline__ void load_d2<float2>(const float2* st, uint64_t i, do
     const float2 v = st[i];
     re = v.x;
     im = v.y;
+}
+
+// |a|^2 of one amplitude as a double-float (h, e): complex128 entries split
+// exactly into float pairs, squares formed with FMA.
+__device__ __forceinline__ void norm2_df(double2 a, float& h, float& e) {
+    const DF r = df_split(a.x), m = df_split(a.y);
+    const float ph = r.h * r.h, qh = m.h * m.h;
+    float pe = fmaf(r.h, r.h, -ph);
+    pe = fmaf(2.f * r.h, r.l, pe);
+    float qe = fmaf(m.h, m.h, -qh);
+    qe = fmaf(2.f * m.h, m.l, qe);
+    h = ph + qh;
+    const float bb = h - ph;
+    e = ((ph - (h - bb)) + (qh - bb)) + pe + qe;
+}
+__device__ __forceinline__ void norm2_df(float2 a, float& h, float& e) {
+    const float ph = a.x * a.x, qh = a.y * a.y;
+    const float pe = fmaf(a.x, a.x, -ph), qe = fmaf(a.y, a.y, -qh);
+    h = ph + qh;
+    const float bb = h - ph;
+    e = ((ph - (h - bb)) + (qh - bb)) + pe + qe;
+}
+
+// sum_i (-1)^popcount(i & z) |a_i|^2: the expectation of a Z string, one read
+// of the state, two amplitudes in flight per thread.
+template <class S>
+__global__ void __launch_bounds__(kThreads) zparity_kernel(const S* __restrict__ state, uint64_t count, uint64_t z,
+                                                           double* __restrict__ partials) {
+    __shared__ double red[32];
+    float sh = 0.f, sl = 0.f;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    auto acc = [&](uint64_t i, S a) {
+        float h, e;
+        norm2_df(a, h, e);
+        if (__popcll(i & z) & 1) {
+            h = -h;
+            e = -e;
+        }
+        const float s = sh + h, bb = s - sh;
+        sl += ((sh - (s - bb)) + (h - bb)) + e;
+        sh = s;
+    };
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    for (; i + stride < count; i += 2 * stride) {
+        const S a0 = state[i], a1 = state[i + stride];
+        acc(i, a0);
+        acc(i + stride, a1);
+    }
+    if (i < count) acc(i, state[i]);
+    double v[1] = {(double)sh + (double)sl};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
 }
 
 template <class S>
@@ -1393,10 +1453,20 @@ cudaError_t block_sums(int arith, const void* state, int n, uint64_t nblocks, do
 
 cudaError_t reduce_pauli_expectation(int arith, const void* state, int n, int nterms, const uint64_t* d_xm,
                                      const uint64_t* d_ym, const uint64_t* d_zm, const double* d_coef,
-                                     ReduceScratch& rs, cudaStream_t s, double* out) {
+                                     ReduceScratch& rs, cudaStream_t s, double* out, bool zonly, uint64_t zmask0) {
     arith = base_arith(arith);
     const uint64_t count = 1ULL << n;
     const int g = reduce_grid(count);
+    if (zonly && nterms == 1) {
+        // one Z string with a real coefficient: a signed norm (coef applied on the host)
+        if (arith == kArithF32)
+            zparity_kernel<float2><<<g, kThreads, 0, s>>>((const float2*)state, count, zmask0, rs.d_partials);
+        else
+            zparity_kernel<double2><<<g, kThreads, 0, s>>>((const double2*)state, count, zmask0, rs.d_partials);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        return finish_reduce<1>(g, rs, s, out);
+    }
     if (arith == kArithF32)
         pauli_expect_kernel<float2><<<g, kThreads, 0, s>>>((const float2*)state, count, nterms, d_xm, d_ym, d_zm,
                                                            d_coef, rs.d_partials);
