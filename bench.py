@@ -206,27 +206,29 @@ def capacity_report():
     """The largest states one GPU holds: 33 qubits complex128 and 34 qubits
     complex64 (128 GiB each). Random layers with CNOT targets biased to the
     top 8 qubits + 4 Grover iterations (multi-controlled Z over all qubits),
-    gates sent one run() each (the engine's pass planner tiles them); timed
-    forward, then the inverse circuit must return |0...0>."""
+    greedy fusion k <= 5 (the multi-controlled Z gates stay single-gate
+    clusters); timed forward, then the inverse stream must return |0...0>."""
     import hiqsimulator_gb300 as hqs
     from hiqsimulator_gb300 import circuits
     out = {}
     for prec, n in (("c128", 33), ("c64", 34)):
         gates, _ = circuits.capacity_circuit(seed=99, n=n)
         qs = list(range(n))
+        clusters = circuits.greedy_clusters(gates, qs, 5)
         sim = hqs.SimulatorMPI(99, n, 5, prec)
         sim.allocate_qureg(qs, 0)
         sim.synchronize()
         sim.enable_pass_timing(True)
         sim.timer_start()
-        circuits.replay(sim, circuits.fusion_off_stream(gates))
+        circuits.replay(sim, circuits.greedy_stream(gates, qs, 5, clusters=clusters))
         ms = sim.timer_stop()
         pt = sim.pass_timing()
         sim.enable_pass_timing(False)
         norm = sim.get_probability([], [])
-        circuits.replay(sim, circuits.fusion_off_stream(circuits.inverse(gates)))
+        circuits.replay(sim, circuits.inverse_stream(gates, clusters))
         p0 = abs(sim.get_amplitude([False] * n, qs)) ** 2
         out[prec] = {"qubits": n, "state_bytes": (16 if prec == "c128" else 8) << n, "gates": len(gates),
+                     "fused_gates": len(clusters),
                      "ms": ms, "passes": pt["launches"], "pass_bytes": pt["bytes"],
                      "pass_GBs": pt["bytes"] / (pt["ms"] / 1e3) / 1e9 if pt["ms"] > 0 else None,
                      "norm_after_circuit": norm, "round_trip_p0": p0}

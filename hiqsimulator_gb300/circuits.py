@@ -199,6 +199,18 @@ def inverse(gates):
     return [Gate(np.conj(np.asarray(g.matrix)).T.copy(), list(g.ids), list(g.ctrls)) for g in reversed(gates)]
 
 
+def inverse_stream(gates, clusters):
+    """Command stream of the inverse circuit that undoes a clustered stream
+    cluster by cluster: the clusters in reverse order, each cluster's gates
+    reversed and inverted, then run()."""
+    cmds = []
+    for cl in reversed(clusters):
+        for g in inverse([gates[i] for i in cl]):
+            cmds.append(("gate", g))
+        cmds.append(("run",))
+    return cmds
+
+
 def pauli_sum(seed, n, terms=8):
     """Random Pauli-string sum with real N(0,1) coefficients, in the backend's
     encoding [(term, coef)] with term = [(index, 'X'|'Y'|'Z'), ...]."""
