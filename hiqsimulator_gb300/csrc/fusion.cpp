@@ -36,7 +36,8 @@ void Fusion::insert(DenseGate g, const std::vector<int64_t>& ctrls) {
 }
 
 void Fusion::handle_controls(DenseGate& g, const std::vector<int64_t>& ctrls) {
-    std::set<int64_t> unhandled = ctrl_set_;
+    if (ctrls.empty() && ctrl_set_.empty()) return;
+    IdSet unhandled = ctrl_set_;
     for (int64_t c : ctrls) {
         if (ctrl_set_.count(c) == 0) {
             if (!items_.empty()) {
@@ -67,39 +68,47 @@ void Fusion::perform(DenseGate& out, std::vector<int64_t>& ctrls) {
     out.m.assign((size_t)dim * dim, cplx(0.0, 0.0));
     for (int i = 0; i < dim; ++i) out.m[(size_t)i * dim + i] = factor_;
     out.diag = true;
-    std::vector<cplx> col(dim);
     for (const auto& it : items_) {
         if (!it.diag) out.diag = false;
         const int k = (int)it.ids.size();
-        std::vector<int> bit(k);
-        for (int l = 0; l < k; ++l)
-            bit[l] = (int)(std::lower_bound(out.ids.begin(), out.ids.end(), it.ids[l]) - out.ids.begin());
+        const int D = 1 << k;
+        // off[j]: the fused-matrix row offset of item row / column j; x: the
+        // gathered rows (on the stack up to 5 qubits, the largest a pass runs)
+        constexpr int kStack = 32;
+        uint32_t off_s[kStack];
+        cplx x_s[kStack];
+        std::vector<uint32_t> off_h;
+        std::vector<cplx> x_h;
+        uint32_t* off = off_s;
+        cplx* x = x_s;
+        if (D > kStack) {
+            off_h.resize(D);
+            x_h.resize(D);
+            off = off_h.data();
+            x = x_h.data();
+        }
+        for (int j = 0; j < D; ++j) off[j] = 0;
         uint32_t itmask = 0;
-        for (int l = 0; l < k; ++l) itmask |= 1u << bit[l];
-        // local index of every row of the fused matrix within the item
-        std::vector<int> loc(dim);
-        for (int i = 0; i < dim; ++i) {
-            int li = 0;
-            for (int l = 0; l < k; ++l) li |= ((i >> bit[l]) & 1) << l;
-            loc[i] = li;
+        for (int l = 0; l < k; ++l) {
+            const uint32_t b = 1u << (std::lower_bound(out.ids.begin(), out.ids.end(), it.ids[l]) - out.ids.begin());
+            itmask |= b;
+            for (int j = 0; j < D; ++j)
+                if ((j >> l) & 1) off[j] |= b;
         }
-        std::vector<int> scatter(1 << k);
-        // new M[:, c] = (item (x) I) old M[:, c]
-        for (int c = 0; c < dim; ++c) {
-            for (int i = 0; i < dim; ++i) col[i] = out.m[(size_t)i * dim + c];
-            for (int i = 0; i < dim; ++i) {
-                const int li = loc[i];
-                const uint32_t base = (uint32_t)i & ~itmask;
-                cplx acc(0.0, 0.0);
-                for (int j = 0; j < (1 << k); ++j) {
-                    uint32_t src = base;
-                    for (int l = 0; l < k; ++l)
-                        if ((j >> l) & 1) src |= 1u << bit[l];
-                    acc += col[src] * it.m[(size_t)li * it.dim + j];
+        // new M[:, c] = (item (x) I) old M[:, c]: per column, each group of D
+        // rows that differ only in the item's bits is gathered, multiplied by
+        // the item and written back (the same products, summed in the same
+        // order, as row by row)
+        for (int c = 0; c < dim; ++c)
+            for (uint32_t base = 0; base < (uint32_t)dim; ++base) {
+                if (base & itmask) continue;
+                for (int j = 0; j < D; ++j) x[j] = out.m[(size_t)(base | off[j]) * dim + c];
+                for (int jo = 0; jo < D; ++jo) {
+                    cplx acc(0.0, 0.0);
+                    for (int j = 0; j < D; ++j) acc += x[j] * it.m[(size_t)jo * it.dim + j];
+                    out.m[(size_t)(base | off[jo]) * dim + c] = acc;
                 }
-                out.m[(size_t)i * dim + c] = acc;
             }
-        }
     }
     ctrls.assign(ctrl_set_.begin(), ctrl_set_.end());
     factor_ = 1.0;

@@ -11,6 +11,7 @@
 #include <complex>
 #include <cstdint>
 #include <set>
+#include <algorithm>
 #include <vector>
 
 namespace hqs {
@@ -30,6 +31,25 @@ void add_controls(DenseGate& g, const std::vector<int64_t>& ctrls);
 // Exact diagonality test on the unfolded matrix (funcs.hpp:325-337).
 bool is_diagonal(const std::vector<cplx>& m, int dim);
 
+// Sorted set of qubit ids in a flat vector (a fused gate holds at most a few).
+struct IdSet {
+    std::vector<int64_t> v;
+    void insert(int64_t x) {
+        auto it = std::lower_bound(v.begin(), v.end(), x);
+        if (it == v.end() || *it != x) v.insert(it, x);
+    }
+    size_t count(int64_t x) const { return std::binary_search(v.begin(), v.end(), x) ? 1 : 0; }
+    void erase(int64_t x) {
+        auto it = std::lower_bound(v.begin(), v.end(), x);
+        if (it != v.end() && *it == x) v.erase(it);
+    }
+    bool empty() const { return v.empty(); }
+    size_t size() const { return v.size(); }
+    void clear() { v.clear(); }
+    std::vector<int64_t>::const_iterator begin() const { return v.begin(); }
+    std::vector<int64_t>::const_iterator end() const { return v.end(); }
+};
+
 class Fusion {
 public:
     // fusion_mpi.hpp:85-99: a 1x1 matrix only scales the fused gate.
@@ -45,9 +65,9 @@ public:
 private:
     void handle_controls(DenseGate& g, const std::vector<int64_t>& ctrls);
 
-    std::set<int64_t> set_;
+    IdSet set_;
     std::vector<DenseGate> items_;
-    std::set<int64_t> ctrl_set_;
+    IdSet ctrl_set_;
     cplx factor_ = 1.0;
 };
 

@@ -45,14 +45,28 @@ Server::Server(int precision, int arith, uint64_t budget_bytes, int max_active, 
     if (arith_ == 0) arith_ = precision_ == 1 ? kArithTC64 : kArithTC;
     if (precision_ == 1 && arith_ == kArithTC) arith_ = kArithTC64;
     if ((precision_ == 1) != arith_is_c64(arith_)) throw std::invalid_argument("server: precision/arith mismatch");
-    for (int i = 0; i < 2; ++i) cuda_check(cudaEventCreateWithFlags(&staging_done_[i], cudaEventDisableTiming), "cudaEventCreate");
+    for (int i = 0; i < 2; ++i)
+        cuda_check(cudaEventCreateWithFlags(&staging_done_[i], cudaEventDisableTiming), "cudaEventCreate");
+    cuda_check(cudaEventCreateWithFlags(&step_done_, cudaEventDisableTiming), "cudaEventCreate");
+    cuda_check(cudaEventRecord(step_done_, ws_.stream()), "cudaEventRecord");
+    cuda_check(cudaEventCreateWithFlags(&freed_, cudaEventDisableTiming), "cudaEventCreate");
     cuda_check(cudaMalloc(&blocks_dev_, sizeof(double) << 15), "cudaMalloc(blocks)");
     cuda_check(cudaMallocHost(&blocks_host_, sizeof(double) << 15), "cudaMallocHost(blocks)");
     t0_ = 0;
     t0_ = now();
+    const unsigned hw = std::thread::hardware_concurrency();
+    const unsigned nw = std::max(1u, std::min(8u, hw > 1 ? hw - 1 : 1u));
+    for (unsigned i = 0; i < nw; ++i) workers_.emplace_back(&Server::worker, this);
 }
 
 Server::~Server() {
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        stop_ = true;
+    }
+    cv_work_.notify_all();
+    for (auto& t : workers_) t.join();
+    cudaStreamSynchronize(wsr_.stream());
     cudaStreamSynchronize(ws_.stream());
     for (auto& r : active_)
         if (r.state) cudaFreeAsync(r.state, ws_.stream());
@@ -62,6 +76,8 @@ Server::~Server() {
         cudaFree(dev_[i]);
         cudaEventDestroy(staging_done_[i]);
     }
+    cudaEventDestroy(step_done_);
+    cudaEventDestroy(freed_);
     cudaFree(blocks_dev_);
     cudaFreeHost(blocks_host_);
 }
@@ -75,6 +91,15 @@ uint64_t Server::submit(int n, const std::vector<ServerGate>& gates, int kind, d
                         const std::vector<uint64_t>& pauli_x, const std::vector<uint64_t>& pauli_y,
                         const std::vector<uint64_t>& pauli_z, const std::vector<cplx>& pauli_coef) {
     if (n < 1 || n > 40) throw std::invalid_argument("server: qubit count out of range");
+    for (const auto& sg : gates) {
+        const int dim = 1 << sg.targets.size();
+        if ((size_t)dim * dim != sg.m.size()) throw std::invalid_argument("server: matrix size does not match targets");
+        if ((int)sg.targets.size() > kMaxK) throw std::invalid_argument("server: a gate acts on more than 5 qubits");
+        for (int t : sg.targets)
+            if (t < 0 || t >= n) throw std::invalid_argument("server: target out of range");
+        for (int c : sg.ctrls)
+            if (c < 0 || c >= n) throw std::invalid_argument("server: control out of range");
+    }
     Req r;
     r.id = next_id_++;
     r.n = n;
@@ -86,9 +111,23 @@ uint64_t Server::submit(int n, const std::vector<ServerGate>& gates, int kind, d
     r.pc = pauli_coef;
     r.bytes = ((uint64_t)1 << n) * (precision_ == 1 ? 8 : 16);
     r.submit_s = now();
-    // Sequential greedy fusion: gates join the current fused gate while the
-    // union of their qubits stays within cluster_; controlled gates too large
-    // to fuse go alone with their controls as a control mask.
+    r.prep = std::make_shared<Prep>();
+    r.prep->n = n;
+    r.prep->gates = gates;
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        jobs_.push_back(r.prep);
+    }
+    cv_work_.notify_one();
+    queue_.push_back(std::move(r));
+    return queue_.back().id;
+}
+
+// Sequential greedy fusion: gates join the current fused gate while the union
+// of their qubits stays within cluster_; controlled gates too large to fuse go
+// alone with their controls as a control mask. Then the tensor-core pools of
+// the gates that will run on the tensor cores.
+void Server::prepare(Prep& p) const {
     Fusion fu;
     uint64_t cur = 0;
     auto flush = [&]() {
@@ -97,22 +136,15 @@ uint64_t Server::submit(int n, const std::vector<ServerGate>& gates, int kind, d
         std::vector<int64_t> ctrls;
         fu.perform(g, ctrls);
         GateOp op;
-        if (to_gate_op(g, ctrls, op)) r.ops.push_back(std::move(op));
+        if (to_gate_op(g, ctrls, op)) p.ops.push_back(std::move(op));
         fu.clear();
         cur = 0;
     };
-    for (const auto& sg : gates) {
+    for (const auto& sg : p.gates) {
         const int dim = 1 << sg.targets.size();
-        if ((size_t)dim * dim != sg.m.size()) throw std::invalid_argument("server: matrix size does not match targets");
         uint64_t q = 0;
-        for (int t : sg.targets) {
-            if (t < 0 || t >= n) throw std::invalid_argument("server: target out of range");
-            q |= 1ULL << t;
-        }
-        for (int c : sg.ctrls) {
-            if (c < 0 || c >= n) throw std::invalid_argument("server: control out of range");
-            q |= 1ULL << c;
-        }
+        for (int t : sg.targets) q |= 1ULL << t;
+        for (int c : sg.ctrls) q |= 1ULL << c;
         DenseGate g;
         g.dim = dim;
         g.m = sg.m;
@@ -131,12 +163,35 @@ uint64_t Server::submit(int n, const std::vector<ServerGate>& gates, int kind, d
         cur |= q;
     }
     flush();
-    // digit planes of tensor-core-sized gates once, not every round
     if (arith_has_tc(arith_))
-        for (auto& op : r.ops)
+        for (auto& op : p.ops)
             if (tc_candidate(arith_, op)) op.tc_pool = make_tc_pool(arith_, op);
-    queue_.push_back(std::move(r));
-    return queue_.back().id;
+    p.gates.clear();
+    p.gates.shrink_to_fit();
+}
+
+void Server::worker() {
+    for (;;) {
+        std::shared_ptr<Prep> job;
+        {
+            std::unique_lock<std::mutex> lk(mu_);
+            cv_work_.wait(lk, [&] { return stop_ || (!jobs_.empty() && prepared_waiting_ < kPrepAhead); });
+            if (stop_) return;
+            job = jobs_.front();
+            jobs_.pop_front();
+        }
+        try {
+            prepare(*job);
+        } catch (...) {
+            job->error = std::current_exception();
+        }
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            job->ready.store(true, std::memory_order_release);
+            ++prepared_waiting_;
+        }
+        cv_ready_.notify_all();
+    }
 }
 
 ServerResult Server::finish(Req& r) {
@@ -146,7 +201,7 @@ ServerResult Server::finish(Req& r) {
     res.submit_s = r.submit_s;
     res.admit_s = r.admit_s;
     res.passes = r.passes;
-    cudaStream_t s = ws_.stream();
+    cudaStream_t s = wsr_.stream();
     const size_t eb = precision_ == 1 ? 8 : 16;
     if (r.kind == kResultAmplitude0) {
         if (eb == 8) {
@@ -207,10 +262,10 @@ ServerResult Server::finish(Req& r) {
         }
         double out = 0.0;
         if (T > 0) {
-            const unsigned char* d = static_cast<const unsigned char*>(ws_.upload(blob.data(), blob.size()));
+            const unsigned char* d = static_cast<const unsigned char*>(wsr_.upload(blob.data(), blob.size()));
             cuda_check(reduce_pauli_expectation(arith_, r.state, r.n, (int)T, (const uint64_t*)d,
                                                 (const uint64_t*)(d + T * 8), (const uint64_t*)(d + 2 * T * 8),
-                                                (const double*)(d + 3 * T * 8), ws_.reduce(), s, &out),
+                                                (const double*)(d + 3 * T * 8), wsr_.reduce(), s, &out),
                        "reduce_pauli_expectation");
         }
         res.value_re = out;
@@ -225,28 +280,14 @@ ServerResult Server::finish(Req& r) {
 std::vector<ServerResult> Server::step() {
     std::vector<ServerResult> done;
     cudaStream_t s = ws_.stream();
-    // 1. finish circuits whose last pass was launched in an earlier round
-    std::vector<Req> keep;
-    keep.reserve(active_.size());
-    for (auto& r : active_) {
-        if (r.next >= r.ops.size()) done.push_back(finish(r));
-        else keep.push_back(std::move(r));
-    }
-    active_.swap(keep);
-    // 2. admit waiting requests in arrival order while memory and slots allow
-    while (!queue_.empty() && (int)active_.size() < max_active_ && bytes_in_use_ + queue_.front().bytes <= budget_) {
-        Req r = std::move(queue_.front());
-        queue_.pop_front();
-        cuda_check(cudaMallocAsync(&r.state, r.bytes, s), "cudaMallocAsync(state)");
-        cuda_check(cudaMemsetAsync(r.state, 0, r.bytes, s), "cudaMemsetAsync");
-        cuda_check(fill_value(arith_, r.state, 1, 1.0, 0.0, s), "fill_value");
-        bytes_in_use_ += r.bytes;
-        r.admit_s = now();
-        active_.push_back(std::move(r));
-    }
+    // circuits whose last pass ran in an earlier round finish after this
+    // round's launches, overlapping them
+    std::vector<size_t> finishing;
+    for (size_t i = 0; i < active_.size(); ++i)
+        if (active_[i].next >= active_[i].ops.size()) finishing.push_back(i);
     if (!queue_.empty() && active_.empty() && queue_.front().bytes > budget_)
         throw std::runtime_error("server: a request needs more HBM than the admission budget");
-    // 3. plan the next pass of every resident circuit
+    // 1. plan the next pass of every resident circuit
     struct Planned {
         Req* r;
         PassPlan plan;
@@ -267,7 +308,7 @@ std::vector<ServerResult> Server::step() {
         ++r.passes;
         planned.push_back(p);
     }
-    // 4. one launch per (kernel, shared-memory class): a launch runs at the
+    // 2. one launch per (kernel, shared-memory class): a launch runs at the
     // occupancy of its largest pass, so passes are grouped by footprint
     auto smem_class = [](size_t b) { return b <= 56 * 1024 ? 0 : b <= 75 * 1024 ? 1 : b <= 112 * 1024 ? 2 : 3; };
     std::stable_sort(planned.begin(), planned.end(), [&](const Planned& a, const Planned& b) {
@@ -331,12 +372,60 @@ std::vector<ServerResult> Server::step() {
         lo = hi;
     }
     ++rounds_;
+    // 3. results of the circuits collected above: the results stream waits
+    // for the end of the previous step (the round that ran their last passes
+    // and every admission before it), not for this step's round
+    if (!finishing.empty()) {
+        cudaStream_t sr = wsr_.stream();
+        cuda_check(cudaStreamWaitEvent(sr, step_done_, 0), "cudaStreamWaitEvent");
+        std::vector<char> gone(active_.size(), 0);
+        for (size_t i : finishing) {
+            done.push_back(finish(active_[i]));
+            gone[i] = 1;
+        }
+        // new states may reuse the freed memory once the frees are ordered
+        // before the main stream's next allocations
+        cuda_check(cudaEventRecord(freed_, sr), "cudaEventRecord");
+        cuda_check(cudaStreamWaitEvent(s, freed_, 0), "cudaStreamWaitEvent");
+        std::vector<Req> keep;
+        keep.reserve(active_.size());
+        for (size_t i = 0; i < active_.size(); ++i)
+            if (!gone[i]) keep.push_back(std::move(active_[i]));
+        active_.swap(keep);
+    }
+    // 4. admit waiting requests in arrival order, once prepared, while memory
+    // and slots allow; they join the next round
+    while (!queue_.empty() && (int)active_.size() < max_active_ && bytes_in_use_ + queue_.front().bytes <= budget_ &&
+           queue_.front().prep->ready.load(std::memory_order_acquire)) {
+        Req r = std::move(queue_.front());
+        queue_.pop_front();
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            --prepared_waiting_;
+        }
+        cv_work_.notify_one();
+        if (r.prep->error) std::rethrow_exception(r.prep->error);
+        r.ops = std::move(r.prep->ops);
+        r.prep.reset();
+        cuda_check(cudaMallocAsync(&r.state, r.bytes, s), "cudaMallocAsync(state)");
+        cuda_check(cudaMemsetAsync(r.state, 0, r.bytes, s), "cudaMemsetAsync");
+        cuda_check(fill_value(arith_, r.state, 1, 1.0, 0.0, s), "fill_value");
+        bytes_in_use_ += r.bytes;
+        r.admit_s = now();
+        active_.push_back(std::move(r));
+    }
+    cuda_check(cudaEventRecord(step_done_, s), "cudaEventRecord");
     return done;
 }
 
 std::vector<ServerResult> Server::drain() {
     std::vector<ServerResult> all;
     while (!queue_.empty() || !active_.empty()) {
+        if (active_.empty()) {
+            // nothing on the GPU: wait for the next request's preparation
+            std::unique_lock<std::mutex> lk(mu_);
+            cv_ready_.wait(lk, [&] { return queue_.front().prep->ready.load(std::memory_order_acquire); });
+        }
         std::vector<ServerResult> d = step();
         all.insert(all.end(), d.begin(), d.end());
     }

@@ -10,16 +10,24 @@
 // resident circuit that still has gates, the next tiled pass of its fused
 // gates (the same planner as the single-state engine) and runs all of them in
 // one batched launch, so circuits admitted while others are in flight share
-// the GPU from their first round on. A circuit whose last pass has been
-// launched is finished in the next round: its result is computed on the
-// device, read back, and its memory is released, which admits waiting
-// requests. Results do not depend on which other circuits share a round.
+// the GPU. A circuit whose last pass has been launched is finished in the
+// next round, after that round's launches: its result is computed on a second
+// stream that waits only for the round that ran its last pass (so the host
+// reads results while the GPU runs the next round), then its memory is
+// released, which admits waiting requests. Results do not depend on which
+// other circuits share a round.
 #pragma once
 #include <cuda_runtime.h>
 
+#include <atomic>
+#include <condition_variable>
 #include <cstdint>
 #include <deque>
+#include <exception>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "fusion.h"
@@ -52,9 +60,12 @@ public:
     Server(const Server&) = delete;
     Server& operator=(const Server&) = delete;
 
-    // Fuses the gates on the host (consecutive gates while their qubits fit
-    // in cluster_size) and queues the request. pauli_* describe the Pauli sum
-    // for kResultExpectation (x/y/z masks over qubit indices, complex coefs).
+    // Checks the gates and queues the request; worker threads fuse them on
+    // the host (consecutive gates while their qubits fit in cluster_size) and
+    // precompute the tensor-core pools while earlier requests run, and the
+    // request is admitted, in arrival order, once that is done. pauli_*
+    // describe the Pauli sum for kResultExpectation (x/y/z masks over qubit
+    // indices, complex coefs).
     uint64_t submit(int n, const std::vector<ServerGate>& gates, int kind, double rnd,
                     const std::vector<uint64_t>& pauli_x, const std::vector<uint64_t>& pauli_y,
                     const std::vector<uint64_t>& pauli_z, const std::vector<cplx>& pauli_coef);
@@ -70,11 +81,20 @@ public:
     cudaStream_t stream() const { return ws_.stream(); }
 
 private:
+    // Host preparation of one request, filled by a worker thread.
+    struct Prep {
+        int n = 0;
+        std::vector<ServerGate> gates;
+        std::vector<GateOp> ops;
+        std::exception_ptr error;
+        std::atomic<bool> ready{false};
+    };
     struct Req {
         uint64_t id;
         int n;
         int kind;
         double rnd;
+        std::shared_ptr<Prep> prep;  // until admitted
         std::vector<GateOp> ops;
         size_t next = 0;
         std::vector<uint64_t> px, py, pz;
@@ -86,13 +106,18 @@ private:
     };
     ServerResult finish(Req& r);
     double now() const;
+    void prepare(Prep& p) const;
+    void worker();
 
     int precision_, arith_, max_active_, cluster_;
     uint64_t budget_, bytes_in_use_ = 0;
     uint64_t next_id_ = 1, rounds_ = 0, launches_ = 0;
     std::deque<Req> queue_;
     std::vector<Req> active_;
-    Workspace ws_;
+    Workspace ws_;   // rounds: planning uploads, batched launches, admissions
+    Workspace wsr_;  // results of finished circuits
+    cudaEvent_t step_done_ = nullptr;  // end of the previous step (its round and admissions)
+    cudaEvent_t freed_ = nullptr;      // after the last frees on the results stream
     void* staging_[2] = {nullptr, nullptr};  // pinned: items + matrices
     size_t staging_bytes_[2] = {0, 0};
     cudaEvent_t staging_done_[2] = {nullptr, nullptr};
@@ -103,6 +128,15 @@ private:
     double* blocks_host_ = nullptr;
     std::vector<std::complex<double>> scan_;
     double t0_;
+    // preparation workers: FIFO jobs, at most kPrepAhead prepared requests
+    // waiting for admission
+    static constexpr size_t kPrepAhead = 256;
+    std::mutex mu_;
+    std::condition_variable cv_work_, cv_ready_;
+    std::deque<std::shared_ptr<Prep>> jobs_;
+    size_t prepared_waiting_ = 0;
+    bool stop_ = false;
+    std::vector<std::thread> workers_;
 };
 
 }  // namespace hqs
