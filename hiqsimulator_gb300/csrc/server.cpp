@@ -300,7 +300,13 @@ std::vector<ServerResult> Server::step() {
         if (r.next >= r.ops.size()) continue;
         const size_t window = std::min<size_t>(r.ops.size() - r.next, kMaxOpsPerPass);
         std::vector<size_t> first;
-        std::vector<PassPlan> plans = plan_passes(r.n, arith_, r.ops.data() + r.next, window, 10, 16, &first, 1);
+        // small states: tiles up to 2^12 amplitudes (the planner shrinks them
+        // to fit shared memory) and up to 24 gates, so a circuit needs few
+        // rounds (host work grows with the passes planned). complex128
+        // tensor-core passes keep their occupancy: their digit scratch grows
+        // with the tile, and a batched launch runs at its largest item's
+        std::vector<PassPlan> plans = plan_passes(r.n, arith_, r.ops.data() + r.next, window, kMaxTileBits,
+                                                  kMaxOpsPerPass, &first, 1, arith_ == kArithTC);
         plans[0].desc.prefetch = 0;  // the batched kernel loads its tiles directly
         Planned p{&r, plans[0], r.next, pass_has_tc(plans[0].desc), 0};
         p.smem = pass_smem_bytes(arith_, p.plan.desc);
