@@ -303,10 +303,12 @@ std::vector<ServerResult> Server::step() {
         // small states: tiles up to 2^12 amplitudes (the planner shrinks them
         // to fit shared memory) and up to 24 gates, so a circuit needs few
         // rounds (host work grows with the passes planned). complex128
-        // tensor-core passes keep their occupancy: their digit scratch grows
-        // with the tile, and a batched launch runs at its largest item's
+        // tensor-core passes keep their first gate's occupancy: their digit
+        // scratch grows with the tile, and a batched launch runs at its
+        // largest item's (measured: 109 circuits/s against 104 at a floor of
+        // 2 CTAs per SM and 86 with no floor)
         std::vector<PassPlan> plans = plan_passes(r.n, arith_, r.ops.data() + r.next, window, kMaxTileBits,
-                                                  kMaxOpsPerPass, &first, 1, arith_ == kArithTC);
+                                                  kMaxOpsPerPass, &first, 1, arith_ == kArithTC ? -1 : 0);
         plans[0].desc.prefetch = 0;  // the batched kernel loads its tiles directly
         Planned p{&r, plans[0], r.next, pass_has_tc(plans[0].desc), 0};
         p.smem = pass_smem_bytes(arith_, p.plan.desc);

@@ -247,7 +247,7 @@ static int pass_ctas(int arith, const PassDesc& d) {
 }
 
 std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t nops, int max_tile_bits, int max_ops,
-                                  std::vector<size_t>* op_first, size_t max_passes, bool keep_occupancy) {
+                                  std::vector<size_t>* op_first, size_t max_passes, int min_ctas) {
     const size_t melem = Workspace::mat_elem_bytes(arith);
     // staged matrices per pass; 3xTF32 passes take two 5-qubit gates
     const size_t mat_budget = (arith == kArithTF32 ? 72 : 64) * 1024;
@@ -276,8 +276,9 @@ std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t no
         PassPlan pl = build_pass(n, arith, ops, i, j, max_tile_bits);
         // leave out trailing ops whose matrices would cost a resident CTA per
         // SM: the pass then runs at the occupancy of its first op
-        if (keep_occupancy && j - i > 1) {
-            const int best = pass_ctas(arith, build_pass(n, arith, ops, i, i + 1, max_tile_bits).desc);
+        if (min_ctas != 0 && j - i > 1) {
+            int best = pass_ctas(arith, build_pass(n, arith, ops, i, i + 1, max_tile_bits).desc);
+            if (min_ctas > 0) best = std::min(best, min_ctas);
             while (j - i > 1 && pass_ctas(arith, pl.desc) < best) {
                 --j;
                 pl = build_pass(n, arith, ops, i, j, max_tile_bits);

@@ -107,12 +107,14 @@ size_t pass_pool_bytes(int arith, const PassDesc& d);
 void write_pass_pool(int arith, const PassDesc& d, const GateOp* ops, unsigned char* dst);
 
 // Build the pass descriptors for ops (exposed for host-side tests of the planner).
-// keep_occupancy: leave out trailing ops that would cost a resident CTA per
-// SM (the right trade when a sweep is expensive; batched serving of small
-// states, bound by host work per pass, turns it off).
+// min_ctas: trailing ops that would bring the pass below this many resident
+// CTAs per SM (or below its first op's, if fewer) start the next pass; -1
+// keeps the first op's occupancy (the right trade when a sweep is
+// expensive), 0 never leaves ops out (batched serving of small states, bound
+// by host work per pass).
 std::vector<PassPlan> plan_passes(int n, int arith, const GateOp* ops, size_t nops, int max_tile_bits, int max_ops,
                                   std::vector<size_t>* op_first = nullptr, size_t max_passes = SIZE_MAX,
-                                  bool keep_occupancy = true);
+                                  int min_ctas = -1);
 inline std::vector<PassPlan> plan_passes(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits,
                                          int max_ops, std::vector<size_t>* op_first = nullptr) {
     return plan_passes(n, arith, ops.data(), ops.size(), max_tile_bits, max_ops, op_first);
