@@ -474,6 +474,12 @@ int hqs_server_info(const hqs_server* srv, uint64_t out[5]) {
     return HQS_OK;
 }
 
+int hqs_server_timing(const hqs_server* srv, double out[6]) {
+    if (!srv || !out) return HQS_ERR_INVALID;
+    srv->srv->timing(out);
+    return HQS_OK;
+}
+
 // ----------------------------------------------------------- kernel level
 
 int hqs_ws_create(hqs_ws** out) {

@@ -125,18 +125,19 @@ uint64_t Server::submit(int n, const std::vector<ServerGate>& gates, int kind, d
 
 // Sequential greedy fusion: gates join the current fused gate while the union
 // of their qubits stays within cluster_; controlled gates too large to fuse go
-// alone with their controls as a control mask. Then the tensor-core pools of
-// the gates that will run on the tensor cores.
+// alone with their controls as a control mask. Then the passes and their
+// matrix pools.
 void Server::prepare(Prep& p) const {
     Fusion fu;
     uint64_t cur = 0;
+    std::vector<GateOp> ops;
     auto flush = [&]() {
         if (fu.empty()) return;
         DenseGate g;
         std::vector<int64_t> ctrls;
         fu.perform(g, ctrls);
         GateOp op;
-        if (to_gate_op(g, ctrls, op)) p.ops.push_back(std::move(op));
+        if (to_gate_op(g, ctrls, op)) ops.push_back(std::move(op));
         fu.clear();
         cur = 0;
     };
@@ -163,11 +164,29 @@ void Server::prepare(Prep& p) const {
         cur |= q;
     }
     flush();
-    if (arith_has_tc(arith_))
-        for (auto& op : p.ops)
-            if (tc_candidate(arith_, op)) op.tc_pool = make_tc_pool(arith_, op);
     p.gates.clear();
     p.gates.shrink_to_fit();
+    // plan every pass: small states take tiles up to 2^12 amplitudes (the
+    // planner shrinks them to fit shared memory) and up to 24 gates, so a
+    // circuit needs few rounds. complex128 tensor-core passes keep their first
+    // gate's occupancy: their digit scratch grows with the tile, and a batched
+    // launch runs at its largest item's (measured: 109 circuits/s against 104
+    // at a floor of 2 CTAs per SM and 86 with no floor)
+    std::vector<size_t> first;
+    p.plans = plan_passes(p.n, arith_, ops.data(), ops.size(), kMaxTileBits, kMaxOpsPerPass, &first, SIZE_MAX,
+                          arith_ == kArithTC ? -1 : 0);
+    size_t total = 256;
+    for (const auto& pl : p.plans) total = std::max(total, pl.pool_off + pass_pool_bytes(arith_, pl.desc));
+    p.pool.assign(total, 0);
+    p.plan_tc.resize(p.plans.size());
+    p.plan_smem.resize(p.plans.size());
+    for (size_t k = 0; k < p.plans.size(); ++k) {
+        PassDesc& d = p.plans[k].desc;
+        d.prefetch = 0;  // the batched kernel loads its tiles directly
+        write_pass_pool(arith_, d, ops.data() + first[k], p.pool.data() + p.plans[k].pool_off);
+        p.plan_tc[k] = pass_has_tc(d) ? 1 : 0;
+        p.plan_smem[k] = (uint32_t)pass_smem_bytes(arith_, d);
+    }
 }
 
 void Server::worker() {
@@ -278,43 +297,29 @@ ServerResult Server::finish(Req& r) {
 }
 
 std::vector<ServerResult> Server::step() {
+    const double t_start = now();
     std::vector<ServerResult> done;
     cudaStream_t s = ws_.stream();
     // circuits whose last pass ran in an earlier round finish after this
     // round's launches, overlapping them
     std::vector<size_t> finishing;
     for (size_t i = 0; i < active_.size(); ++i)
-        if (active_[i].next >= active_[i].ops.size()) finishing.push_back(i);
+        if (active_[i].next >= active_[i].prep->plans.size()) finishing.push_back(i);
     if (!queue_.empty() && active_.empty() && queue_.front().bytes > budget_)
         throw std::runtime_error("server: a request needs more HBM than the admission budget");
-    // 1. plan the next pass of every resident circuit
+    // 1. the next pass of every resident circuit (planned at preparation)
     struct Planned {
         Req* r;
-        PassPlan plan;
-        size_t first;
+        size_t k;
         bool tc;
         size_t smem;
     };
     std::vector<Planned> planned;
     for (auto& r : active_) {
-        if (r.next >= r.ops.size()) continue;
-        const size_t window = std::min<size_t>(r.ops.size() - r.next, kMaxOpsPerPass);
-        std::vector<size_t> first;
-        // small states: tiles up to 2^12 amplitudes (the planner shrinks them
-        // to fit shared memory) and up to 24 gates, so a circuit needs few
-        // rounds (host work grows with the passes planned). complex128
-        // tensor-core passes keep their first gate's occupancy: their digit
-        // scratch grows with the tile, and a batched launch runs at its
-        // largest item's (measured: 109 circuits/s against 104 at a floor of
-        // 2 CTAs per SM and 86 with no floor)
-        std::vector<PassPlan> plans = plan_passes(r.n, arith_, r.ops.data() + r.next, window, kMaxTileBits,
-                                                  kMaxOpsPerPass, &first, 1, arith_ == kArithTC ? -1 : 0);
-        plans[0].desc.prefetch = 0;  // the batched kernel loads its tiles directly
-        Planned p{&r, plans[0], r.next, pass_has_tc(plans[0].desc), 0};
-        p.smem = pass_smem_bytes(arith_, p.plan.desc);
-        r.next += (size_t)plans[0].desc.nops;
+        if (r.next >= r.prep->plans.size()) continue;
+        planned.push_back(Planned{&r, r.next, r.prep->plan_tc[r.next] != 0, r.prep->plan_smem[r.next]});
+        ++r.next;
         ++r.passes;
-        planned.push_back(p);
     }
     // 2. one launch per (kernel, shared-memory class): a launch runs at the
     // occupancy of its largest pass, so passes are grouped by footprint
@@ -328,10 +333,13 @@ std::vector<ServerResult> Server::step() {
         const size_t nitems = hi - lo;
         const size_t head = ((nitems * sizeof(BatchItem)) + 255) & ~(size_t)255;
         size_t total = head;
-        for (size_t i = lo; i < hi; ++i) total += pass_pool_bytes(arith_, planned[i].plan.desc);
+        for (size_t i = lo; i < hi; ++i)
+            total += pass_pool_bytes(arith_, planned[i].r->prep->plans[planned[i].k].desc);
         const int f = flip_;
         flip_ ^= 1;
+        const double tw = now();
         cuda_check(cudaEventSynchronize(staging_done_[f]), "cudaEventSynchronize");
+        t_phase_[1] += now() - tw;
         if (staging_bytes_[f] < total) {
             cudaFreeHost(staging_[f]);
             staging_[f] = nullptr;
@@ -354,21 +362,24 @@ std::vector<ServerResult> Server::step() {
         uint64_t tiles = 0;
         size_t smem = 0;
         for (size_t i = lo; i < hi; ++i) {
-            const PassDesc& d = planned[i].plan.desc;
+            const PassPlan& pl = planned[i].r->prep->plans[planned[i].k];
+            const PassDesc& d = pl.desc;
             BatchItem& b = bi[i - lo];
             b.state = planned[i].r->state;
             b.mats = dev + off;
             b.tile_begin = tiles;
             b.desc = d;
-            write_pass_pool(arith_, d, planned[i].r->ops.data() + planned[i].first, host + off);
+            std::memcpy(host + off, planned[i].r->prep->pool.data() + pl.pool_off, pass_pool_bytes(arith_, d));
             off += pass_pool_bytes(arith_, d);
             tiles += 1ULL << (d.n - d.nins);
             smem = std::max(smem, planned[i].smem);
         }
+        const double tl = now();
         cuda_check(cudaMemcpyAsync(dev, host, total, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(batch)");
         cuda_check(cudaEventRecord(staging_done_[f], s), "cudaEventRecord");
         cuda_check(launch_batch(arith_, tc, reinterpret_cast<const BatchItem*>(dev), (int)nitems, tiles, smem, s),
                    "launch_batch");
+        t_phase_[2] += now() - tl;
         ++launches_;
     };
     for (size_t lo = 0; lo < planned.size();) {
@@ -380,6 +391,8 @@ std::vector<ServerResult> Server::step() {
         lo = hi;
     }
     ++rounds_;
+    const double t_res = now();
+    t_phase_[0] += t_res - t_start;  // batching, waits and launches (split below)
     // 3. results of the circuits collected above: the results stream waits
     // for the end of the previous step (the round that ran their last passes
     // and every admission before it), not for this step's round
@@ -401,6 +414,8 @@ std::vector<ServerResult> Server::step() {
             if (!gone[i]) keep.push_back(std::move(active_[i]));
         active_.swap(keep);
     }
+    const double t_adm = now();
+    t_phase_[3] += t_adm - t_res;
     // 4. admit waiting requests in arrival order, once prepared, while memory
     // and slots allow; they join the next round
     while (!queue_.empty() && (int)active_.size() < max_active_ && bytes_in_use_ + queue_.front().bytes <= budget_ &&
@@ -413,8 +428,6 @@ std::vector<ServerResult> Server::step() {
         }
         cv_work_.notify_one();
         if (r.prep->error) std::rethrow_exception(r.prep->error);
-        r.ops = std::move(r.prep->ops);
-        r.prep.reset();
         cuda_check(cudaMallocAsync(&r.state, r.bytes, s), "cudaMallocAsync(state)");
         cuda_check(cudaMemsetAsync(r.state, 0, r.bytes, s), "cudaMemsetAsync");
         cuda_check(fill_value(arith_, r.state, 1, 1.0, 0.0, s), "fill_value");
@@ -423,6 +436,9 @@ std::vector<ServerResult> Server::step() {
         active_.push_back(std::move(r));
     }
     cuda_check(cudaEventRecord(step_done_, s), "cudaEventRecord");
+    const double t_end = now();
+    t_phase_[4] += t_end - t_adm;
+    t_phase_[5] += t_end - t_start;
     return done;
 }
 

@@ -78,14 +78,25 @@ public:
     uint64_t bytes_in_use() const { return bytes_in_use_; }
     uint64_t rounds() const { return rounds_; }
     uint64_t launches() const { return launches_; }
+    // host seconds in step(): batching, staging waits, launches, results,
+    // admissions, total
+    void timing(double out[6]) const {
+        for (int i = 0; i < 6; ++i) out[i] = t_phase_[i];
+        out[0] -= t_phase_[1] + t_phase_[2];
+    }
     cudaStream_t stream() const { return ws_.stream(); }
 
 private:
-    // Host preparation of one request, filled by a worker thread.
+    // Host preparation of one request, filled by a worker thread: the fused
+    // gates planned into passes, and every pass's matrices already in the
+    // kernels' format in one host pool (pass k at plans[k].pool_off).
     struct Prep {
         int n = 0;
         std::vector<ServerGate> gates;
-        std::vector<GateOp> ops;
+        std::vector<PassPlan> plans;
+        std::vector<uint8_t> plan_tc;      // pass runs tensor-core gates
+        std::vector<uint32_t> plan_smem;   // shared-memory bytes of the pass
+        std::vector<unsigned char> pool;
         std::exception_ptr error;
         std::atomic<bool> ready{false};
     };
@@ -94,8 +105,7 @@ private:
         int n;
         int kind;
         double rnd;
-        std::shared_ptr<Prep> prep;  // until admitted
-        std::vector<GateOp> ops;
+        std::shared_ptr<Prep> prep;  // the request's passes; next = first pass not yet launched
         size_t next = 0;
         std::vector<uint64_t> px, py, pz;
         std::vector<cplx> pc;
@@ -106,6 +116,7 @@ private:
     };
     ServerResult finish(Req& r);
     double now() const;
+    double t_phase_[6] = {0, 0, 0, 0, 0, 0};
     void prepare(Prep& p) const;
     void worker();
 

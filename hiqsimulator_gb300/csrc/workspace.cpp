@@ -116,7 +116,9 @@ static size_t tc_scratch_bytes(int arith, int q, int k) {
 
 // Dense gates that run on the tensor cores: k >= 3 for complex128 (the
 // double-float alternative costs ~10 FP32 operations per real product);
-// k = 5 only for complex64, whose FP32 gates are cheap enough below that
+// k = 5 only for complex64, whose FP32 gates are cheaper below that (measured
+// in serving of <= 4-qubit fused gates: 174 circuits/s with 4-qubit gates on
+// the tensor cores against 279 on FP32 cores)
 bool tc_candidate(int arith, const GateOp& op) {
     if (!arith_has_tc(arith) || op.diag) return false;
     return op.k >= (arith == kArithTC ? 3 : 5);

@@ -42,6 +42,7 @@ def _lib():
                                           _P(_u64), _P(_u64), _P(_u64), _P(_d), _P(_u64)]
         lib.hqs_server_step.argtypes = [_vp, _P(ServerResult), _sz, _P(_sz)]
         lib.hqs_server_info.argtypes = [_vp, _P(_u64)]
+        lib.hqs_server_timing.argtypes = [_vp, _P(_d)]
         lib._server_bound = True
     return lib
 
@@ -138,6 +139,12 @@ class Server:
         out = (_u64 * 5)()
         self._check(self.lib.hqs_server_info(self.h, out))
         return dict(zip(("queued", "active", "bytes_in_use", "rounds", "launches"), list(out)))
+
+    def timing(self):
+        """Host seconds spent in step(), by phase."""
+        out = (_d * 6)()
+        self._check(self.lib.hqs_server_timing(self.h, out))
+        return dict(zip(("batching", "staging_wait", "launch", "results", "admission", "step"), list(out)))
 
     def drain(self):
         res = []

@@ -213,6 +213,11 @@ int hqs_server_submit(hqs_server* srv, int n, int ngates, const int* ntgt, const
 int hqs_server_step(hqs_server* srv, hqs_server_result* out, size_t cap, size_t* n);
 /* queued, resident, bytes in use, rounds, launches */
 int hqs_server_info(const hqs_server* srv, uint64_t out[5]);
+/* Host seconds spent in step() since creation: out[0] batching (items and
+ * matrix staging), out[1] waiting for a staging buffer to be free, out[2]
+ * launches, out[3] results of finished circuits, out[4] admissions, out[5]
+ * all of step(). No reference counterpart (diagnostics of the server). */
+int hqs_server_timing(const hqs_server* srv, double out[6]);
 
 /* ------------------------------------------------------------------------
  * Kernel-level API on device memory (one fused gate / reduction per call).
