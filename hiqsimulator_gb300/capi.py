@@ -87,8 +87,42 @@ def load():
     lib.hqs_ws_synchronize.argtypes = [_vp]
     lib.hqs_ws_timer_start.argtypes = [_vp]
     lib.hqs_ws_timer_stop.argtypes = [_vp, _P(ctypes.c_float)]
+    lib.hqs_plan_passes.argtypes = [_i, _i, _i, _P(_i), _P(_i), _P(_u64), _P(_i), _i, _i, _P(PassInfo), _sz,
+                                    _P(_sz)]
     _lib = lib
     return lib
+
+
+class PassInfo(ctypes.Structure):
+    _fields_ = [("first_op", ctypes.c_uint32), ("nops", ctypes.c_uint32), ("q", ctypes.c_uint32),
+                ("w", ctypes.c_uint32), ("prefetch", ctypes.c_uint32), ("tc_ops", ctypes.c_uint32),
+                ("tile_mask", ctypes.c_uint64), ("fixed_mask", ctypes.c_uint64), ("smem_bytes", ctypes.c_uint64),
+                ("pool_bytes", ctypes.c_uint64), ("sweep_bytes", ctypes.c_uint64)]
+
+
+def _gate_arrays(gates):
+    """(k, positions, ctrl_mask, diag, ...) tuples as the C ABI's arrays."""
+    nops = len(gates)
+    k = np.array([g[0] for g in gates] or [0], dtype=np.int32)
+    pos = np.zeros(max(nops, 1) * 5, dtype=np.int32)
+    ctrl = np.array([g[2] for g in gates] or [0], dtype=np.uint64)
+    diag = np.array([1 if g[3] else 0 for g in gates] or [0], dtype=np.int32)
+    for i, g in enumerate(gates):
+        pos[5 * i:5 * i + g[0]] = g[1]
+    return nops, k, pos, ctrl, diag
+
+
+def plan_passes(n, arith, gates, max_tile_bits=0, max_ops=0):
+    """How the engine groups gates (k, positions, ctrl_mask, diag[, matrix])
+    into tiled passes, computed on the host: a list of dicts (PassInfo fields)."""
+    lib = load()
+    nops, k, pos, ctrl, diag = _gate_arrays(gates)
+    cap = max(nops, 1)
+    out = (PassInfo * cap)()
+    np_ = _sz()
+    check_ws(lib.hqs_plan_passes(n, ARITH[arith], nops, _ptr(k, _i), _ptr(pos, _i), _ptr(ctrl, _u64),
+                                 _ptr(diag, _i), max_tile_bits, max_ops, out, cap, ctypes.byref(np_)))
+    return [{f: getattr(out[i], f) for f, _ in PassInfo._fields_} for i in range(np_.value)]
 
 
 def _ptr(a, t):

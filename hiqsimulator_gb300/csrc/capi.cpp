@@ -519,35 +519,75 @@ static void check_state_args(const void* state, int n, int arith) {
     need(arith >= HQS_ARITH_F64 && arith <= HQS_ARITH_TC64, "unknown arithmetic");
 }
 
+// Gates in the kernel-level array form (see hqs_apply_gates) as GateOps;
+// mats may be null (zero matrices of the right sizes, for planning only).
+static std::vector<hqs::GateOp> ops_from_arrays(int n, int nops, const int* k, const int* pos, const uint64_t* ctrl,
+                                                const int* diag, const double* mats) {
+    std::vector<hqs::GateOp> ops(nops);
+    size_t off = 0;
+    for (int i = 0; i < nops; ++i) {
+        hqs::GateOp& op = ops[i];
+        need(k[i] >= 0 && k[i] <= hqs::kMaxK && k[i] <= n, "gate size out of range");
+        op.k = k[i];
+        op.diag = diag[i] != 0;
+        op.ctrl_mask = (k[i] == 0) ? 0 : ctrl[i];
+        uint64_t seen = 0;
+        for (int j = 0; j < k[i]; ++j) {
+            const int p = pos[5 * i + j];
+            need(p >= 0 && p < n, "target position out of range");
+            need(!((seen >> p) & 1ULL), "repeated target position");
+            need(!((op.ctrl_mask >> p) & 1ULL), "a target is also a control");
+            seen |= 1ULL << p;
+            op.pos[j] = p;
+        }
+        need(n >= 64 || (op.ctrl_mask >> n) == 0, "control position out of range");
+        const size_t cnt = (k[i] == 0) ? 1 : (op.diag ? (1u << k[i]) : (1u << (2 * k[i])));
+        op.m.assign(cnt, hqs::cplx(0.0, 0.0));
+        if (mats) std::memcpy(static_cast<void*>(op.m.data()), mats + 2 * off, cnt * sizeof(hqs::cplx));
+        off += cnt;
+    }
+    return ops;
+}
+
+int hqs_plan_passes(int n, int arith, int nops, const int* k, const int* pos, const uint64_t* ctrl, const int* diag,
+                    int max_tile_bits, int max_ops, hqs_pass_info* out, size_t cap, size_t* npasses) {
+    return guarded(g_err, [&]() {
+        need(n >= 1 && n <= 40, "n out of range");
+        need(arith >= HQS_ARITH_F64 && arith <= HQS_ARITH_TC64, "unknown arithmetic");
+        need(nops >= 0 && (nops == 0 || (k && pos && ctrl && diag)), "null gate arrays");
+        need(npasses && (cap == 0 || out), "null output");
+        const std::vector<hqs::GateOp> ops = ops_from_arrays(n, nops, k, pos, ctrl, diag, nullptr);
+        std::vector<size_t> first;
+        const std::vector<hqs::PassPlan> plans = hqs::plan_passes(
+            n, arith, ops, max_tile_bits > 0 ? max_tile_bits : 11, max_ops > 0 ? max_ops : 16, &first);
+        *npasses = plans.size();
+        for (size_t p = 0; p < plans.size() && p < cap; ++p) {
+            const hqs::PassDesc& d = plans[p].desc;
+            hqs_pass_info& o = out[p];
+            o.first_op = (uint32_t)first[p];
+            o.nops = (uint32_t)d.nops;
+            o.q = (uint32_t)d.q;
+            o.w = (uint32_t)d.w;
+            o.prefetch = d.prefetch;
+            o.tc_ops = 0;
+            for (int i = 0; i < d.nops; ++i) o.tc_ops += d.ops[i].tc;
+            o.tile_mask = 0;
+            for (int i = 0; i < d.q; ++i) o.tile_mask |= 1ULL << d.tile_pos[i];
+            o.fixed_mask = d.fixed_mask;
+            o.smem_bytes = hqs::pass_smem_bytes(arith, d);
+            o.pool_bytes = hqs::pass_pool_bytes(arith, d);
+            o.sweep_bytes = plans[p].bytes;
+        }
+    });
+}
+
 int hqs_apply_gates(hqs_ws* ws, void* state, int n, int arith, int nops, const int* k, const int* pos,
                     const uint64_t* ctrl, const int* diag, const double* mats, int max_tile_bits, int max_ops,
                     uint64_t* bytes_out, uint64_t* passes_out) {
     WS_CALL(ws, {
         check_state_args(state, n, arith);
         need(nops >= 0 && (nops == 0 || (k && pos && ctrl && diag && mats)), "null gate arrays");
-        std::vector<hqs::GateOp> ops(nops);
-        size_t off = 0;
-        for (int i = 0; i < nops; ++i) {
-            hqs::GateOp& op = ops[i];
-            need(k[i] >= 0 && k[i] <= hqs::kMaxK && k[i] <= n, "gate size out of range");
-            op.k = k[i];
-            op.diag = diag[i] != 0;
-            op.ctrl_mask = (k[i] == 0) ? 0 : ctrl[i];
-            uint64_t seen = 0;
-            for (int j = 0; j < k[i]; ++j) {
-                const int p = pos[5 * i + j];
-                need(p >= 0 && p < n, "target position out of range");
-                need(!((seen >> p) & 1ULL), "repeated target position");
-                need(!((op.ctrl_mask >> p) & 1ULL), "a target is also a control");
-                seen |= 1ULL << p;
-                op.pos[j] = p;
-            }
-            need(n >= 64 || (op.ctrl_mask >> n) == 0, "control position out of range");
-            const size_t cnt = (k[i] == 0) ? 1 : (op.diag ? (1u << k[i]) : (1u << (2 * k[i])));
-            op.m.resize(cnt);
-            std::memcpy(static_cast<void*>(op.m.data()), mats + 2 * off, cnt * sizeof(hqs::cplx));
-            off += cnt;
-        }
+        std::vector<hqs::GateOp> ops = ops_from_arrays(n, nops, k, pos, ctrl, diag, mats);
         uint64_t passes = 0;
         const uint64_t bytes = ws->ws->apply_ops(state, n, arith, ops, max_tile_bits > 0 ? max_tile_bits : 11,
                                                  max_ops > 0 ? max_ops : 16, &passes);

@@ -237,6 +237,22 @@ void hqs_ws_destroy(hqs_ws* ws);
  * k == 0. Gates are grouped into tiled passes of at most max_tile_bits tile
  * bits and max_ops gates (0 = defaults). *bytes_out (optional) receives the
  * algorithmic HBM bytes, *passes_out (optional) the number of sweeps. */
+/* How hqs_apply_gates would group the same gates into passes, computed on
+ * the host (no GPU, no matrices needed). No reference counterpart (the
+ * reference runs one sweep per fused gate). *npasses receives the count;
+ * the first cap passes are described in out. */
+typedef struct {
+    uint32_t first_op, nops;   /* the pass applies gates [first_op, first_op + nops) */
+    uint32_t q, w;             /* tile bits; tile positions 0..w-1 are the contiguous low run */
+    uint32_t prefetch;         /* 0 none, 1 staging buffer, 2 every gate in place, second tile buffer */
+    uint32_t tc_ops;           /* gates on the tensor cores */
+    uint64_t tile_mask;        /* state positions in the tile */
+    uint64_t fixed_mask;       /* control positions outside the tile every gate shares */
+    uint64_t smem_bytes, pool_bytes, sweep_bytes;
+} hqs_pass_info;
+int hqs_plan_passes(int n, int arith, int nops, const int* k, const int* pos, const uint64_t* ctrl, const int* diag,
+                    int max_tile_bits, int max_ops, hqs_pass_info* out, size_t cap, size_t* npasses);
+
 int hqs_apply_gates(hqs_ws* ws, void* state, int n, int arith, int nops, const int* k, const int* pos,
                     const uint64_t* ctrl, const int* diag, const double* mats, int max_tile_bits, int max_ops,
                     uint64_t* bytes_out, uint64_t* passes_out);
