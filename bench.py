@@ -417,7 +417,7 @@ def run_ours(args, dist):
         circuits.replay(sim, cmds)
         force_permutation(sim)
         sim.synchronize()
-    clocks = ClockSampler(dist.local)
+    clocks = ClockSampler(args.gpu_id)
     dist.barrier()
     clocks.start()
     s0 = sim.stats()
@@ -512,7 +512,21 @@ def run_ours(args, dist):
     return 0
 
 
+def bind_gpu():
+    """One GPU per rank under torchrun: the rank's device becomes the only
+    visible one (before any CUDA use in this process). Returns the physical
+    GPU id for nvidia-smi."""
+    ws, _, local = dist_env()
+    vis = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    if ws <= 1:
+        return vis[0] if vis else "0"
+    dev = vis[local % len(vis)] if vis else str(local)
+    os.environ["CUDA_VISIBLE_DEVICES"] = dev
+    return dev
+
+
 def main():
+    gpu_id = bind_gpu()
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
@@ -530,6 +544,7 @@ def main():
     ap.add_argument("--capacity", action="store_true", help="also run the 33q c128 / 34q c64 capacity states")
     ap.add_argument("--table", action="store_true", help="also time the reference-against-GPU table rows")
     args = ap.parse_args()
+    args.gpu_id = gpu_id
     global N_QUBITS
     N_QUBITS = args.qubits
     dist = Dist()

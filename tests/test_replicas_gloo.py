@@ -47,3 +47,18 @@ def test_two_gloo_ranks_max_and_barrier():
     res = sorted(q.get(timeout=5) for _ in range(2))
     assert [r[1] for r in res] == [20.0, 20.0]
     assert [r[2] for r in res] == [0, 0]
+
+
+def test_each_rank_sees_only_its_gpu(monkeypatch):
+    sys.path.insert(0, ROOT)
+    import bench
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    monkeypatch.setenv("RANK", "1")
+    monkeypatch.setenv("LOCAL_RANK", "1")
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "4,5")
+    assert bench.bind_gpu() == "5" and os.environ["CUDA_VISIBLE_DEVICES"] == "5"
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES")
+    assert bench.bind_gpu() == "1" and os.environ["CUDA_VISIBLE_DEVICES"] == "1"
+    monkeypatch.setenv("WORLD_SIZE", "1")
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "3")
+    assert bench.bind_gpu() == "3" and os.environ["CUDA_VISIBLE_DEVICES"] == "3"
