@@ -328,6 +328,19 @@ int hqs_sim_info(const hqs_sim* sim, int* precision, int* arith) {
     return HQS_OK;
 }
 
+int hqs_sim_state_view(hqs_sim* sim, void** state, uint64_t* amplitudes, int* device) {
+    SIM_CALL(sim, {
+        need(state && amplitudes, "null output");
+        sim->eng->synchronize();
+        void* p = sim->eng->device_state();
+        cudaPointerAttributes attr{};
+        hqs::cuda_check(cudaPointerGetAttributes(&attr, p), "cudaPointerGetAttributes");
+        *state = p;
+        *amplitudes = 1ULL << sim->eng->num_qubits();
+        if (device) *device = attr.device;
+    });
+}
+
 int hqs_sim_timer_start(hqs_sim* sim) {
     SIM_CALL(sim, {
         sim->eng->flush();

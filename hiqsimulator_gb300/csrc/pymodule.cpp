@@ -57,6 +57,61 @@ std::string env_or(const char* name, const char* dflt) {
     return (v && *v) ? std::string(v) : std::string(dflt);
 }
 
+// DLPack exchange structures (unversioned ABI, DLPack 0.8), laid out as the
+// DLPack specification defines them, so that torch.from_dlpack / cupy adopt
+// the state without a copy from a capsule named "dltensor".
+struct DLDevice {
+    int32_t device_type;  // 2 = CUDA
+    int32_t device_id;
+};
+struct DLDataType {
+    uint8_t code;  // 5 = complex
+    uint8_t bits;
+    uint16_t lanes;
+};
+struct DLTensor {
+    void* data;
+    DLDevice device;
+    int32_t ndim;
+    DLDataType dtype;
+    int64_t* shape;
+    int64_t* strides;
+    uint64_t byte_offset;
+};
+struct DLManagedTensor {
+    DLTensor dl_tensor;
+    void* manager_ctx;
+    void (*deleter)(DLManagedTensor*);
+};
+
+// Owns one exported view: its shape/strides and a reference to the Python
+// simulator object, which keeps the device state allocated while a consumer
+// holds the view.
+struct StateView {
+    DLManagedTensor t{};
+    int64_t shape[1] = {0};
+    int64_t strides[1] = {1};
+    PyObject* owner = nullptr;
+};
+
+void state_view_deleter(DLManagedTensor* t) {
+    StateView* v = static_cast<StateView*>(t->manager_ctx);
+    if (v->owner && Py_IsInitialized()) {
+        // consumers may free the view from a thread without the GIL
+        const PyGILState_STATE g = PyGILState_Ensure();
+        Py_DECREF(v->owner);
+        PyGILState_Release(g);
+    }
+    delete v;
+}
+
+// A capsule that no consumer renamed to "used_dltensor" still owns its view.
+void state_capsule_destructor(PyObject* cap) {
+    if (!PyCapsule_IsValid(cap, "dltensor")) return;
+    auto* t = static_cast<DLManagedTensor*>(PyCapsule_GetPointer(cap, "dltensor"));
+    if (t && t->deleter) t->deleter(t);
+}
+
 struct PauliArgs {
     std::vector<size_t> off{0};
     std::vector<int64_t> idx;
@@ -248,6 +303,34 @@ public:
         d["ms"] = ms;
         return d;
     }
+    // Zero-copy export of the device state (position order) as a DLPack
+    // capsule; owner is the Python object of this simulator.
+    py::object state_dlpack(const py::object& owner) {
+        void* p = nullptr;
+        uint64_t amps = 0;
+        int dev = 0;
+        check(hqs_sim_state_view(h_, &p, &amps, &dev));
+        auto* v = new StateView();
+        v->shape[0] = (int64_t)amps;
+        DLTensor& d = v->t.dl_tensor;
+        d.data = p;
+        d.device = DLDevice{2, dev};
+        d.ndim = 1;
+        d.dtype = DLDataType{5, (uint8_t)(precision() == "c64" ? 64 : 128), 1};
+        d.shape = v->shape;
+        d.strides = v->strides;
+        d.byte_offset = 0;
+        v->t.manager_ctx = v;
+        v->t.deleter = state_view_deleter;
+        v->owner = owner.ptr();
+        Py_INCREF(v->owner);
+        PyObject* cap = PyCapsule_New(&v->t, "dltensor", state_capsule_destructor);
+        if (!cap) {
+            state_view_deleter(&v->t);
+            throw py::error_already_set();
+        }
+        return py::reinterpret_steal<py::object>(cap);
+    }
     void timer_start() { check(hqs_sim_timer_start(h_)); }
     float timer_stop() {
         float ms = 0;
@@ -296,6 +379,7 @@ PYBIND11_MODULE(_cppsim_mpi, m) {
         .def("stats", &SimulatorMPI::stats)
         .def("enable_pass_timing", &SimulatorMPI::enable_pass_timing)
         .def("pass_timing", &SimulatorMPI::pass_timing)
+        .def("state_dlpack", [](py::object self) { return self.cast<SimulatorMPI&>().state_dlpack(self); })
         .def("timer_start", &SimulatorMPI::timer_start)
         .def("timer_stop", &SimulatorMPI::timer_stop)
         .def_property_readonly("precision", &SimulatorMPI::precision)

@@ -151,6 +151,16 @@ int hqs_sim_set_pass_limits(hqs_sim* sim, int max_tile_bits, int max_ops, int de
 int hqs_sim_stats(const hqs_sim* sim, uint64_t out[6]);
 /* Precision and arithmetic of the handle. */
 int hqs_sim_info(const hqs_sim* sim, int* precision, int* arith);
+/* Zero-copy view of the state (the device-side counterpart of cheat_local,
+ * SimulatorMPI.cpp:543-559): launches every pending fused gate, waits for the
+ * device, and returns the device address of the 2^n amplitudes in position
+ * order (interleaved complex128, or interleaved complex64 for HQS_C64), their
+ * count and the CUDA device ordinal. The address stays valid until the handle
+ * is destroyed or a call allocates or deallocates a qubit, applies a qubit
+ * operator or sets the wavefunction; later passes change the contents in
+ * place. Device writes through the view must be complete before the next
+ * call on the handle (the handle's stream does not wait for other streams). */
+int hqs_sim_state_view(hqs_sim* sim, void** state, uint64_t* amplitudes, int* device);
 /* Device timing on the handle's stream: start records an event after every
  * pending fused gate is launched; stop records a second one, waits for it and
  * returns the elapsed milliseconds. */

@@ -450,3 +450,34 @@ def test_c64_fidelity_against_c128_oracle(hqs, cuda, arith):
         assert fid > 1 - 1e-6, fid
         assert abs(norm - 1) < 1e-6, norm
     assert np.max(np.abs(vec - ref.vec)) < 1e-5
+
+
+@pytest.mark.parametrize("precision", ["c128", "c64"])
+def test_state_dlpack_view_is_zero_copy(hqs, cuda, precision):
+    """state_dlpack(): the device state adopted by torch without a copy. It
+    equals cheat_local() bit for bit, shows later passes in place, and keeps
+    the state allocated after the simulator object is dropped."""
+    import gc
+    from hiqsimulator_gb300 import circuits
+    torch = cuda
+    n = 12
+    qs = list(range(n))
+    sim = hqs.SimulatorMPI(3, 24, 4, precision)
+    sim.allocate_qureg(qs, 0)
+    circuits.replay(sim, circuits.greedy_stream(circuits.random_layers(3, qs, 4), qs, 4))
+    sim.run()
+    t = torch.from_dlpack(sim.state_dlpack())
+    assert t.is_cuda and t.shape == (1 << n,)
+    assert t.dtype == (torch.complex128 if precision == "c128" else torch.complex64)
+    _, vec = sim.cheat_local_numpy()
+    assert np.array_equal(t.cpu().numpy(), vec.astype(t.cpu().numpy().dtype))
+    assert torch.from_dlpack(sim.state_dlpack()).data_ptr() == t.data_ptr()
+    unused = sim.state_dlpack()  # a capsule no consumer takes frees its view
+    del unused
+    g1(sim, X, 0)
+    _, vec2 = sim.cheat_local_numpy()
+    assert np.array_equal(t.cpu().numpy(), vec2.astype(t.cpu().numpy().dtype))
+    assert np.max(np.abs(vec2.reshape(-1, 2)[:, ::-1].ravel() - vec)) < (1e-12 if precision == "c128" else 1e-6)
+    del sim
+    gc.collect()
+    assert abs(float(t.abs().square().sum()) - 1) < (1e-12 if precision == "c128" else 1e-5)
