@@ -1,0 +1,39 @@
+"""The benchmark's algorithmic counts on the host: reference bytes and FP64
+flops per fused gate, on hand-built clusters with known answers."""
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import bench  # noqa: E402
+from hiqsimulator_gb300.circuits import H, X, Gate, phase  # noqa: E402
+
+
+def test_cluster_flops_and_bytes_known_answers():
+    n = 10
+    cp = phase(0.3)
+    gates = [
+        Gate(H, [0], []),             # 0
+        Gate(X, [1], [0]),            # 1  CNOT 0 -> 1
+        Gate(cp, [2], [1]),           # 2  controlled phase, diagonal
+        Gate(cp, [3], [4]),           # 3
+        Gate(np.diag([1, 1j]), [5], [6]),  # 4
+        Gate(X, [7], [8, 9]),         # 5  Toffoli
+    ]
+    # {H, CNOT, CP}: dense on qubits {0, 1, 2} (the controls fold into the matrix)
+    assert bench.cluster_flops(gates, [[0, 1, 2]], n) == 8 * 8 * 2 ** n
+    # a lone controlled phase: diagonal on half the state
+    assert bench.cluster_flops(gates, [[3]], n) == 6 * 2 ** (n - 1)
+    # two diagonal gates with different controls: every qubit a target
+    assert bench.cluster_flops(gates, [[3, 4]], n) == 6 * 2 ** n
+    # a Toffoli alone: a 1-qubit dense gate on a quarter of the state
+    assert bench.cluster_flops(gates, [[5]], n) == 8 * 2 * 2 ** (n - 2)
+    assert bench.cluster_flops(gates, [[0, 1, 2], [3], [5]], n) == (
+        8 * 8 * 2 ** n + 6 * 2 ** (n - 1) + 16 * 2 ** (n - 2))
+    # bytes: one read and one write of the state per fused gate; a lone gate
+    # too large to fuse touches 2^-c of it
+    assert bench.cluster_bytes(gates, [[0, 1, 2], [5]], n) == 2 * 2 * 16 * 2 ** n
