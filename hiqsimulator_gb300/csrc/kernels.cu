@@ -299,11 +299,11 @@ __device__ __forceinline__ void mma_f16(float (&c)[4], const uint32_t (&a)[4], u
                  : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// accumulator of digit pair (i, j) and its level i + j
+// accumulator of digit pair (i, j): one per pair of levels i + j <= 2, one for
+// each of levels 3 and 4
 __host__ __device__ constexpr int tc_acc(int i, int j) {
     return (i + j == 0) ? 0 : (i + j == 1) ? 1 + i : (i + j == 2) ? 3 + i : (i + j == 3) ? 6 : 7;
 }
-__host__ __device__ constexpr int tc_level(int a) { return a == 0 ? 0 : a <= 2 ? 1 : a <= 5 ? 2 : a == 6 ? 3 : 4; }
 
 // Digit counts of each amplitude type (state digits A, gate digits B) and
 // the products kept. complex128: five and five, levels 0..4 (above). complex64:
@@ -1544,7 +1544,7 @@ cudaError_t permute_bits(int arith, void* state, int n, int m, const uint8_t* ol
                          cudaStream_t s) {
     arith = base_arith(arith);
     if (m == 0) return cudaSuccess;
-    PermSpec p;
+    PermSpec p{};
     p.n = n;
     // tile: the permuted positions plus the lowest other positions, up to 2^10
     // amplitudes (or the whole state)
