@@ -62,6 +62,7 @@ def load():
     lib.hqs_sim_num_qubits.argtypes = [_vp, _P(_sz)]
     lib.hqs_sim_get_qubits_ids.argtypes = [_vp, _P(_i64), _sz, _P(_sz)]
     lib.hqs_sim_synchronize.argtypes = [_vp]
+    lib.hqs_sim_state_view.argtypes = [_vp, _P(_vp), _P(_u64), _P(_i)]
     lib.hqs_sim_sample.argtypes = [_vp, _u64, _P(_u64)]
     lib.hqs_sim_get_probability.argtypes = [_vp, _P(ctypes.c_uint8), _sz, _P(_i64), _sz, _P(_d)]
     lib.hqs_sim_measure_qubits.argtypes = [_vp, _P(_i64), _sz, _P(ctypes.c_uint8)]

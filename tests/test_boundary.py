@@ -27,7 +27,8 @@ def test_pybind_module_has_reference_methods(hqs):
                    "apply_controlled_gate", "emulate_math", "get_amplitude", "get_probability", "run", "entropy",
                    "cheat_local", "collapse_wavefunction"]
     added = ["get_expectation_value", "apply_qubit_operator", "set_wavefunction"]
-    for m in ref_methods + added:
+    extensions = ["cheat_local_numpy", "state_dlpack", "sample", "synchronize", "move_qubits"]
+    for m in ref_methods + added + extensions:
         assert hasattr(_cppsim_mpi.SimulatorMPI, m), m
 
 
@@ -41,6 +42,10 @@ def test_invalid_arguments_rejected_without_device(hqs):
     assert lib.hqs_apply_gates(None, None, 3, 1, 0, None, None, None, None, None, 0, 0, None, None) == \
         capi.HQS_ERR_INVALID
     assert lib.hqs_sim_run(None) == capi.HQS_ERR_INVALID
+    ptr, amps, dev = ctypes.c_void_p(), ctypes.c_uint64(), ctypes.c_int()
+    assert lib.hqs_sim_state_view(None, ctypes.byref(ptr), ctypes.byref(amps), ctypes.byref(dev)) == \
+        capi.HQS_ERR_INVALID
+    assert b"null simulator" in lib.hqs_last_error()
     assert lib.hqs_version().startswith(b"hiqsimulator_gb300")
 
 
