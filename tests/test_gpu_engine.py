@@ -370,6 +370,36 @@ def test_rng_draws_match_reference(make):
         assert got == outs, seed
 
 
+def test_sample_matches_oracle_draws(make):
+    """sample(shots): one draw per shot from the simulator's MT19937 stream,
+    each resolved by the reference's block-CDF procedure without collapse
+    (SimulatorMPI.cpp:903-964). The oracle takes the same draws in the same
+    order; outcomes agree except where a draw lies within rounding of a CDF
+    boundary (the oracle reports that margin). The stream stays in step: a
+    measurement afterwards agrees too."""
+    from hiqsimulator_gb300 import circuits
+    from oracle.engine import OracleSimulator
+    n, shots = 17, 512
+    qs = list(range(n))
+    cmds = circuits.greedy_stream(circuits.random_layers(21, qs, 5), qs, 4)
+    sim = make(77, 24, 4)
+    ref = OracleSimulator(77, 24, 4)
+    for s in (sim, ref):
+        s.allocate_qureg(qs, 0)
+        circuits.replay(s, cmds)
+        s.run()
+    got = [int(v) for v in sim.sample(shots)]
+    compared = 0
+    for i in range(shots):
+        want = ref.sample_index(ref.rng.uniform())
+        if ref.last_margin > 1e-12:
+            assert got[i] == want, (i, got[i], want)
+            compared += 1
+    assert compared >= shots - 2
+    assert len(set(got)) > shots // 2  # a spread-out state: the draws hit many blocks
+    assert sim.measure_qubits(qs) == ref.measure_qubits(qs)
+
+
 # ------------------------------------------------------ oracle differential
 
 @pytest.mark.parametrize("n,layers,K,seed", [(16, 8, 4, 1), (18, 6, 5, 2), (22, 3, 5, 3)])
