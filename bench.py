@@ -224,6 +224,31 @@ def cpu_sample(cmds, clusters, max_gates, budget_s):
         done, t_total)
 
 
+def host_info():
+    """The host the CPU legs ran on: core count, architecture and CPU model
+    (lscpu's "Model name", else /proc/cpuinfo's)."""
+    import platform
+    info = {"nproc": os.cpu_count(), "machine": platform.machine(), "cpu_model": None}
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().startswith("Model name:"):
+                info["cpu_model"] = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if info["cpu_model"] is None:
+        try:
+            with open("/proc/cpuinfo") as f:
+                for line in f:
+                    if line.lower().startswith("model name"):
+                        info["cpu_model"] = line.split(":", 1)[1].strip()
+                        break
+        except OSError:
+            pass
+    return info
+
+
 def force_permutation(sim):
     """Move the qubits at the top 5 positions to positions 0-4 (one sweep)."""
     top = sim.get_qubits_ids()[-5:]
@@ -420,7 +445,8 @@ def run_reference(args, dist):
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded circuits)",
             "config": {"workload": "QFT30 + 10 random layers, greedy fusion k<=5, complex128, 30 qubits",
                        "sample": desc},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc,
+                             "host": host_info()},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -524,7 +550,7 @@ def run_ours(args, dist):
     if dist.rank == 0 and not args.no_cpu_baseline:
         os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
         v, threads, desc = cpu_sample(cmds, clusters, max_gates=2, budget_s=20.0)
-        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc}
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc, "host": host_info()}
 
     serv = serving_report(args) if (dist.rank == 0 and args.serve > 0) else None
     prec = precision_report() if (dist.rank == 0 and not args.no_precision) else None

@@ -37,3 +37,10 @@ def test_cluster_flops_and_bytes_known_answers():
     # bytes: one read and one write of the state per fused gate; a lone gate
     # too large to fuse touches 2^-c of it
     assert bench.cluster_bytes(gates, [[0, 1, 2], [5]], n) == 2 * 2 * 16 * 2 ** n
+
+
+def test_host_info_names_the_cpu():
+    info = bench.host_info()
+    assert info["nproc"] == os.cpu_count() and info["nproc"] >= 1
+    assert info["machine"] in ("x86_64", "aarch64")
+    assert info["cpu_model"] is None or isinstance(info["cpu_model"], str)
