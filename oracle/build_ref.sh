@@ -8,10 +8,14 @@
 #
 #   REF_FLAGS  extra compiler flags; default "-O2 -fopenmp" (parity build).
 #              The reference's release flags are "-O3 -ffast-math -march=native".
+#   REF_VARIANT  build into oracle/_ref/<variant>/ instead (e.g. "release" with
+#              REF_FLAGS="-O3 -ffast-math -fopenmp" for timing the reference's
+#              own kernels beside the oracle port).
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 SRC="${1:-${HIQ_REFERENCE_SRC:-/root/reference}}"
-OUT="$HERE/_ref"
+OUT="$HERE/_ref${REF_VARIANT:+/$REF_VARIANT}"
+case "${REF_VARIANT:-}" in */*|..*) echo "build_ref: REF_VARIANT must be a plain name"; exit 1;; esac
 FLAGS="${REF_FLAGS:--O2 -fopenmp}"
 if [ ! -f "$SRC/src/simulator-mpi/SimulatorMPI.cpp" ]; then
     echo "build_ref: reference sources not found at $SRC; skipped"; exit 0
