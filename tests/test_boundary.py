@@ -83,3 +83,22 @@ def test_huge_gate_is_its_own_cluster(hqs):
     flat = [i for c in cl for i in c]
     assert sorted(flat) == [0, 1, 2, 3]
     assert [2] in cl
+
+
+def test_integration_ctypes_stub_runs(hqs, monkeypatch):
+    """The ctypes binding printed for maintainers runs as written: it loads
+    libhqs.so, declares the calls it makes, and turns a failed create (no
+    CUDA device here) into RuntimeError with the library's message."""
+    import re
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("checks the no-device error path")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    monkeypatch.chdir(root)
+    text = open(os.path.join(root, "INTEGRATION.md")).read()
+    stub = [b for b in re.findall(r"```python\n(.*?)```", text, re.S) if "ctypes.CDLL" in b]
+    assert len(stub) == 1
+    ns = {}
+    exec(stub[0], ns)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        ns["SimulatorBackend"](1, 20, 4)
