@@ -188,7 +188,7 @@ def measured_peak():
 
 def profile_traffic():
     """DRAM bytes per pass-kernel launch from the committed ncu summary
-    (profiles/pass_kernel_traffic.json), scaled to the 30-qubit state."""
+    (profiles/pass_kernel_traffic.json), scaled to the state's amplitudes."""
     p = os.path.join(ROOT, "profiles", "pass_kernel_traffic.json")
     if not os.path.exists(p):
         return None
@@ -198,7 +198,7 @@ def profile_traffic():
 
 def cpu_sample(cmds, clusters, max_gates, budget_s):
     """The oracle port of the reference engine on the host cores: the first
-    fused gates of the schedule on a fresh 30-qubit state. Returns
+    fused gates of the schedule on a fresh state of N_QUBITS qubits. Returns
     (GB/s, threads, description)."""
     from oracle.engine import OracleSimulator
     sim = OracleSimulator(SEED, N_QUBITS, CLUSTER)
@@ -220,8 +220,8 @@ def cpu_sample(cmds, clusters, max_gates, budget_s):
             break
     byts = done * 2 * (1 << N_QUBITS) * 16
     threads = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
-    return byts / t_total / 1e9, threads, "%d fused gates of the schedule on the 30-qubit state (%.1f s)" % (
-        done, t_total)
+    return byts / t_total / 1e9, threads, "%d fused gates of the schedule on the %d-qubit state (%.1f s)" % (
+        done, N_QUBITS, t_total)
 
 
 def host_info():
@@ -443,7 +443,8 @@ def run_reference(args, dist):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded circuits)",
-            "config": {"workload": "QFT30 + 10 random layers, greedy fusion k<=5, complex128, 30 qubits",
+            "config": {"workload": "QFT%d + 10 random layers, greedy fusion k<=5, complex128, %d qubits" % (
+                           N_QUBITS, N_QUBITS),
                        "sample": desc},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": desc,
                              "host": host_info()},

@@ -44,3 +44,24 @@ def test_host_info_names_the_cpu():
     assert info["nproc"] == os.cpu_count() and info["nproc"] >= 1
     assert info["machine"] in ("x86_64", "aarch64")
     assert info["cpu_model"] is None or isinstance(info["cpu_model"], str)
+
+
+def test_reference_arm_prints_the_contract_line():
+    """bench.py --impl reference (the CPU arm) prints one JSON line with the
+    keys the benchmark contract needs; run here at 16 qubits."""
+    import json
+    import subprocess
+    env = dict(os.environ, OMP_NUM_THREADS="2")
+    out = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--qubits", "16",
+                          "--steps", "1", "--warmup", "0"], capture_output=True, text=True, timeout=600, env=env,
+                         cwd=ROOT)
+    assert out.returncode == 0, out.stderr[-2000:]
+    line = json.loads(out.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["unit"] == "GB/s" and line["value"] > 0
+    assert line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 0
+    cpu = line["cpu_baseline"]
+    assert cpu["value"] == line["value"] and cpu["cores"] == 2 and cpu["kind"] == "port"
+    assert "16-qubit state" in cpu["sample"] and cpu["host"]["nproc"] == os.cpu_count()
+    assert line["e2e"] == {"value": line["value"], "unit": "GB/s", "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
+    assert "16 qubits" in line["config"]["workload"]
