@@ -22,7 +22,6 @@ sample of the same workload: the first fused gates of the schedule on the
 """
 import argparse
 import json
-import math
 import os
 import statistics
 import subprocess

@@ -5,7 +5,6 @@ import ctypes
 import json
 import os
 
-import numpy as np
 import pytest
 
 from conftest import GOLDEN

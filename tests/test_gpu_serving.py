@@ -1,6 +1,5 @@
 """Batched serving: results equal the same circuit run alone, match the
 oracle, and respect the HBM admission budget."""
-import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
