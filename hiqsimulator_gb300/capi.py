@@ -205,6 +205,38 @@ class Workspace:
         return ms.value
 
 
+def fuse(gates):
+    """Host FP64 fusion (hqs_fuse) of gates given as (matrix, ids, ctrls),
+    inserted in order. Returns (matrix, ids, ctrls, diag) of the fused gate:
+    matrix bit l <-> ids[l] (ascending), ctrls the controls every gate
+    shared."""
+    lib = load()
+    n = len(gates)
+    mats = [np.ascontiguousarray(g[0], dtype=np.complex128) for g in gates]
+    dim = np.array([m.shape[0] for m in mats] or [0], dtype=np.uint64)
+    ioff = np.zeros(n + 1, dtype=np.uint64)
+    coff = np.zeros(n + 1, dtype=np.uint64)
+    for i, g in enumerate(gates):
+        ioff[i + 1] = ioff[i] + len(g[1])
+        coff[i + 1] = coff[i] + len(g[2])
+    m = np.concatenate([x.ravel() for x in mats]) if mats else np.zeros(1, dtype=np.complex128)
+    ids = np.array([q for g in gates for q in g[1]] or [0], dtype=np.int64)
+    ctl = np.array([q for g in gates for q in g[2]] or [0], dtype=np.int64)
+    nq = len({q for g in gates for q in list(g[1]) + list(g[2])})  # the fused ids are among these
+    cap = 1 << (2 * min(nq, 12))
+    out = np.zeros(cap, dtype=np.complex128)
+    oids = np.zeros(64, dtype=np.int64)
+    octl = np.zeros(64, dtype=np.int64)
+    nid, nct, dg = _sz(), _sz(), _i()
+    check_ws(lib.hqs_fuse(n, _ptr(m.view(np.float64), _d), _ptr(dim, _sz), _ptr(ids, _i64), _ptr(ioff, _sz),
+                          _ptr(ctl, _i64), _ptr(coff, _sz), _ptr(out.view(np.float64), _d), cap,
+                          _ptr(oids, _i64), 64, ctypes.byref(nid), _ptr(octl, _i64), 64, ctypes.byref(nct),
+                          ctypes.byref(dg)))
+    d = 1 << nid.value
+    return (out[:d * d].reshape(d, d).copy(), [int(x) for x in oids[:nid.value]],
+            [int(x) for x in octl[:nct.value]], bool(dg.value))
+
+
 def greedy_schedule(gates, ctrls, locals_, cluster_size):
     """Native greedy clustering (hqs_greedy_schedule). Returns a list of
     clusters, each a list of gate indices in emission order."""

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <new>
 #include <string>
@@ -387,6 +388,47 @@ int hqs_greedy_schedule(int ngates, const int64_t* tgt, const int* toff, const i
                                             cluster_end);
         if (nc < 0) throw std::runtime_error("CalcPos(): scheduling with 64 or more qubits is not yet supported");
         *nclusters = nc;
+    });
+}
+
+int hqs_fuse(size_t ngates, const double* m, const size_t* dim, const int64_t* ids, const size_t* ioff,
+             const int64_t* ctrls, const size_t* coff, double* out_m, size_t cap_m, int64_t* out_ids,
+             size_t cap_ids, size_t* n_ids, int64_t* out_ctrls, size_t cap_ctrls, size_t* n_ctrls, int* out_diag) {
+    return guarded(g_err, [&]() {
+        need(ngates == 0 || (m && dim && ioff && coff), "null gate arrays");
+        need(out_m && n_ids && n_ctrls && out_diag, "null outputs");
+        hqs::Fusion f;
+        size_t moff = 0;
+        for (size_t g = 0; g < ngates; ++g) {
+            need(ioff[g] <= ioff[g + 1] && coff[g] <= coff[g + 1], "offsets must not decrease");
+            const size_t nt = ioff[g + 1] - ioff[g], nc = coff[g + 1] - coff[g];
+            need(nt == 0 || ids, "null ids");
+            need(nc == 0 || ctrls, "null ctrls");
+            need(nt <= 12 && dim[g] == ((size_t)1 << nt), "a gate's matrix must be 2^targets square");
+            hqs::DenseGate dg;
+            dg.dim = (int)dim[g];
+            dg.m.resize(dim[g] * dim[g]);
+            std::memcpy(static_cast<void*>(dg.m.data()), m + 2 * moff, dg.m.size() * sizeof(hqs::cplx));
+            moff += dg.m.size();
+            dg.diag = hqs::is_diagonal(dg.m, dg.dim);
+            if (nt) dg.ids.assign(ids + ioff[g], ids + ioff[g + 1]);
+            f.insert(std::move(dg), nc ? std::vector<int64_t>(ctrls + coff[g], ctrls + coff[g + 1])
+                                       : std::vector<int64_t>());
+            need(f.num_qubits() <= 12, "at most 12 fused qubits");
+        }
+        hqs::DenseGate out;
+        std::vector<int64_t> oc;
+        f.perform(out, oc);
+        need((size_t)out.dim * out.dim <= cap_m && out.ids.size() <= cap_ids && oc.size() <= cap_ctrls,
+             "output buffers too small");
+        need(out.ids.empty() || out_ids, "null output ids");
+        need(oc.empty() || out_ctrls, "null output ctrls");
+        std::memcpy(out_m, out.m.data(), out.m.size() * sizeof(hqs::cplx));
+        std::copy(out.ids.begin(), out.ids.end(), out_ids);
+        std::copy(oc.begin(), oc.end(), out_ctrls);
+        *n_ids = out.ids.size();
+        *n_ctrls = oc.size();
+        *out_diag = out.diag ? 1 : 0;
     });
 }
 

@@ -183,6 +183,18 @@ int hqs_greedy_schedule(int ngates, const int64_t* tgt, const int* toff, const i
                         int nlocals, const int64_t* locals, int cluster_size, int* order, int* cluster_end,
                         int* nclusters);
 
+/* Host FP64 gate fusion (fusion_mpi.hpp:85-226, SimulatorMPI.cpp:710-815), no
+ * device: gate g is a dim[g] x dim[g] row-major complex128 matrix (the
+ * matrices concatenated in m as interleaved doubles) on targets
+ * ids[ioff[g]..ioff[g+1]) with controls ctrls[coff[g]..coff[g+1]); each is
+ * tested for exact diagonality and inserted in order, then the queue is fused
+ * into one gate: out_m (2^n_ids x 2^n_ids, cap_m complex values), its qubit
+ * ids ascending (matrix bit l <-> out_ids[l]), the controls every gate shared
+ * (ascending) and whether it is diagonal. At most 12 fused qubits. */
+int hqs_fuse(size_t ngates, const double* m, const size_t* dim, const int64_t* ids, const size_t* ioff,
+             const int64_t* ctrls, const size_t* coff, double* out_m, size_t cap_m, int64_t* out_ids,
+             size_t cap_ids, size_t* n_ids, int64_t* out_ctrls, size_t cap_ctrls, size_t* n_ctrls, int* out_diag);
+
 /* ------------------------------------------------------------------------
  * Batched circuit server (no reference counterpart): many independent
  * circuits resident in HBM, admitted in arrival order against a byte budget
