@@ -98,6 +98,35 @@ def build(verbose=False):
     return LIB, PYMOD
 
 
+def build_sanitized():
+    """A copy of libhqs.so whose host C++ (engine, fusion, planner, scheduler,
+    server, C ABI) is built with AddressSanitizer and UndefinedBehaviorSanitizer,
+    linked with the regular kernel objects, in _build/asan/. A process loads it
+    with the sanitizer runtimes preloaded (LD_PRELOAD). Returns its path."""
+    build()
+    out = os.path.join(OBJ, "asan")
+    os.makedirs(out, exist_ok=True)
+    headers = [os.path.join(CSRC, h) for h in HEADERS] + [os.path.join(INCLUDE, "hqs.h")]
+    flags = ["-O1", "-g", "-std=c++17", "-fPIC", "-fsanitize=address,undefined", "-fno-omit-frame-pointer"]
+    jobs, objs = [], []
+    for src in CXX_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(out, src + ".o")
+        objs.append(o)
+        if _stale(o, [s] + headers):
+            jobs.append(["g++"] + flags + ["-I", os.path.join(CUDA_HOME, "include"), "-I", INCLUDE, "-c", s,
+                                           "-o", o])
+    with ThreadPoolExecutor(max_workers=max(2, min(8, os.cpu_count() or 2))) as ex:
+        list(ex.map(_run, jobs))
+    lib = os.path.join(out, "libhqs.so")
+    cu_objs = [os.path.join(OBJ, src + ".o") for src in CU_SOURCES]
+    if _stale(lib, objs + cu_objs):
+        _run([NVCC] + GENCODE + ["-shared", "-Xcompiler", "-fPIC", "-o", lib + ".tmp"] + objs + cu_objs +
+             ["-Xlinker", "-lasan", "-Xlinker", "-lubsan"])
+        os.replace(lib + ".tmp", lib)
+    return lib
+
+
 def clean():
     shutil.rmtree(OBJ, ignore_errors=True)
     for p in (LIB, PYMOD):
