@@ -147,3 +147,45 @@ def test_oracle_matches_live_reference_when_present():
     assert np.max(np.abs(np.array(r.cheat_local()[1]) - o.vec)) < TOL
     assert r.measure_qubits(list(range(n))) == o.measure_qubits(list(range(n)))
     assert abs(r.entropy() - o.entropy()) < 1e-10
+
+
+RELEASE_CHILD = r"""
+import glob, importlib.util, sys
+import numpy as np
+sys.path.insert(0, {root!r})
+from hiqsimulator_gb300 import circuits
+path = glob.glob({rel!r} + "/_cppsim_mpi*.so")[0]
+spec = importlib.util.spec_from_file_location("_cppsim_mpi", path)
+REF = importlib.util.module_from_spec(spec)
+spec.loader.exec_module(REF)
+n = 12
+qs = list(range(n))
+gates = circuits.qft(qs) + circuits.random_layers(13, qs, 4)
+r = REF.SimulatorMPI(3, 20, 4)
+r.allocate_qureg(qs, 0)
+circuits.replay(r, circuits.greedy_stream(gates, qs, 4))
+r.run()
+np.save({out!r}, np.array(r.cheat_local()[1], dtype=complex))
+"""
+
+
+def test_oracle_matches_release_build_when_present(tmp_path):
+    """The reference built with its release flags (-O3 -ffast-math, by
+    REF_VARIANT=release oracle/build_ref.sh) gives the oracle's state too; it
+    loads in a child process (two builds of one pybind11 module cannot share
+    a process)."""
+    import glob
+    import subprocess
+    import sys
+    rel = os.path.join(ROOT, "oracle", "_ref", "release")
+    if not glob.glob(os.path.join(rel, "_cppsim_mpi*.so")):
+        pytest.skip("release build of the reference (oracle/_ref/release) not present on this machine")
+    out = str(tmp_path / "state.npy")
+    r = subprocess.run([sys.executable, "-c", RELEASE_CHILD.format(root=ROOT, rel=rel, out=out)],
+                       capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    n = 12
+    qs = list(range(n))
+    gates = circuits.qft(qs) + circuits.random_layers(13, qs, 4)
+    o = _run_oracle(n, circuits.greedy_stream(gates, qs, 4), 3, 4)
+    assert np.max(np.abs(np.load(out) - o.vec)) < TOL
