@@ -209,7 +209,8 @@ __device__ __forceinline__ void apply_dense(const typename A::comp_t* __restrict
 // of two digits has at most 18 bits and a 2D <= 64 term sum at most 24 bits,
 // so the fp32 accumulation of one digit pair is exact. Pairs (i, j) with
 // i + j <= 2 get their own accumulators, the pairs of levels 3 and 4 share one
-// each, levels >= 5 are dropped (below 2^-46 of the row scale). The epilogue
+// each, levels >= 5 are dropped (for unitary gates up to 2^-45.5 of the row
+// scale, the largest error of the scheme; measured in an exact model). The epilogue
 // converts the eight accumulators to integers and re-assembles doubles with
 // integer operations.
 
