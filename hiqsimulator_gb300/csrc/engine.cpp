@@ -289,13 +289,24 @@ uint64_t Engine::sample_index(double rnd, bool& ok, double* total) {
                    "cudaMemcpyAsync(block)");
         cuda_check(cudaStreamSynchronize(ws_.stream()), "cudaStreamSynchronize");
     }
+    return scan_block(i, K, rnd);
+}
+
+// In-block scan (SimulatorMPI.cpp:950-958) over the host copy of block i:
+// the first index whose running sum reaches rnd. The block CDF comes from
+// device block sums and the scan from a host sum, so rounding can leave the
+// scan just short of rnd; the draw then belongs to the block's last
+// amplitude with nonzero probability (never past the block).
+uint64_t Engine::scan_block(uint64_t i, uint64_t K, double rnd) const {
     double shift = (i > 0) ? block_host_[i - 1] : 0.0;
-    uint64_t k = i * K;
-    for (uint64_t j = 0; j < K; ++j, ++k) {
-        shift += std::norm(scan_host_[j]);
-        if (shift >= rnd) break;
+    uint64_t last = i * K;
+    for (uint64_t j = 0; j < K; ++j) {
+        const double p = std::norm(scan_host_[j]);
+        if (p > 0.0) last = i * K + j;
+        shift += p;
+        if (shift >= rnd) return i * K + j;
     }
-    return k;
+    return last;
 }
 
 // SimulatorMPI.cpp:897-1008.
@@ -364,13 +375,7 @@ void Engine::sample(uint64_t shots, uint64_t* out) {
             }
             loaded = i;
         }
-        double shift = (i > 0) ? block_host_[i - 1] : 0.0;
-        uint64_t k = i * K;
-        for (uint64_t j = 0; j < K; ++j, ++k) {
-            shift += std::norm(scan_host_[j]);
-            if (shift >= rnd[s]) break;
-        }
-        out[s] = k;
+        out[s] = scan_block(i, K, rnd[s]);
     }
 }
 

@@ -106,6 +106,7 @@ private:
     void pauli_masks(const std::vector<PauliTerm>& terms, const std::vector<int64_t>& ids,
                      std::vector<uint64_t>& xm, std::vector<uint64_t>& ym, std::vector<uint64_t>& zm) const;
     uint64_t sample_index(double rnd, bool& ok, double* total);
+    uint64_t scan_block(uint64_t i, uint64_t K, double rnd) const;
     size_t elem_bytes() const { return precision_ == kC64 ? 8 : 16; }
     int n() const { return (int)locals_.size(); }
 

@@ -297,10 +297,11 @@ int hqs_drop_bit(hqs_ws* ws, void* state, int n, int arith, int pos, int keep);
  * cudaStream_t, NULL for the legacy default stream), asynchronously; nothing
  * is allocated, freed or synchronized. For code that runs under a foreign
  * memory pool or inside recorded launch sequences, where cudaMalloc is not
- * allowed. Limit: at most 2^32 amplitudes matching (mask, val) per call;
- * larger requests fail with HQS_ERR_INVALID. All calls on a device share the
- * array, so calls that overlap on the GPU race; the first call on a device
- * looks the array up and should come before any stream capture. */
+ * allowed. Limit: states of at most 2^40 amplitudes (n <= 40); larger
+ * requests fail with HQS_ERR_INVALID before any launch. All calls on a device
+ * share the array, so calls that overlap on the GPU race; the first call on a
+ * device looks the array up and should come before any stream capture, and
+ * the entry point must not be used on a device after cudaDeviceReset. */
 int hqs_probability_noalloc(const void* state, int n, int arith, uint64_t mask, uint64_t val, double* d_out,
                             void* stream);
 /* Wait for the workspace's stream. */

@@ -13,9 +13,12 @@ hiqsimulator_gb300.circuits and stores what they return:
   ref_rng.json       first uniform draws of std::mt19937(seed) as used by
                      MeasureQubits (one draw per call, read back via outcomes)
   ref_errors.json    error messages of the reference for invalid calls
+  ref_perm_init.json qubit-id getters before and after set_qubits_perm
+                     relabelling, with the queries that follow it; states
+                     after allocate_qureg with a nonzero fill value
 
 Usage (needs the reference sources and a built oracle/_ref):
-    bash oracle/build_ref.sh && python tests/golden/make_golden.py
+    bash oracle/build_ref.sh && python tests/golden/make_golden.py [--only perm_init]
 """
 import json
 import os
@@ -65,7 +68,63 @@ def stream(gates, n, mode, K):
     return circuits.greedy_stream(gates, list(range(n)), K, clusters=ref_schedule(G, C, list(range(n)), K))
 
 
+def cplx_list(vec):
+    return [[float(v.real), float(v.imag)] for v in vec]
+
+
+def perm_init_fixture():
+    """set_qubits_perm relabels positions without moving data
+    (SimulatorMPI.cpp:661-667); the getters return locals_ ++ globals_
+    (:652-679). allocate_qureg(ids, init) fills every amplitude with init
+    (:218-251)."""
+    out = {}
+    n = 6
+    gates = circuits.random_layers(55, list(range(n)), 3)
+    cmds = stream(gates, n, "greedy", 4)
+    sim = REF.SimulatorMPI(55, 24, 4)
+    ids = [3, 0, 5, 1, 4, 2]
+    sim.allocate_qureg(ids, 0)
+    circuits.replay(sim, cmds)
+    sim.run()
+    before = {"ids": list(sim.get_qubits_ids()), "local": list(sim.get_local_qubits_ids()),
+              "global": list(sim.get_global_qubits_ids())}
+    perm = [2, 4, 0, 5, 1, 3]
+    sim.set_qubits_perm(perm)
+    id2pos, vec = sim.cheat_local()
+    bits = [[bool((b >> j) & 1) for j in range(n)] for b in (0, 5, 22, 63)]
+    out["perm"] = {"n": n, "alloc_ids": ids, "seed": 55, "layers": 3, "cluster": 4, "before": before,
+                   "perm": perm,
+                   "after": {"ids": list(sim.get_qubits_ids()), "local": list(sim.get_local_qubits_ids()),
+                             "global": list(sim.get_global_qubits_ids())},
+                   "id2pos": {str(k): int(v) for k, v in id2pos.items()},
+                   "state": cplx_list(vec),
+                   "p1": [sim.get_probability([True], [q]) for q in range(n)],
+                   "amp_bits": bits,
+                   "amp_ids": list(range(n)),
+                   "amps": cplx_list([sim.get_amplitude(b, list(range(n))) for b in bits]),
+                   "p_pair": sim.get_probability([True, False], [4, 1])}
+    fills = []
+    for init, nq in ((0.25, 4), (complex(0.25, -0.25), 3), (complex(0.0, 0.5), 2)):  # normalised states
+        sim = REF.SimulatorMPI(7, 24, 4)
+        sim.allocate_qureg(list(range(nq)), init)
+        filled = cplx_list(sim.cheat_local()[1])
+        g = circuits.random_layers(8, list(range(nq)), 2)
+        circuits.replay(sim, stream(g, nq, "greedy", 4))
+        sim.run()
+        fills.append({"init": [init.real, init.imag] if isinstance(init, complex) else [init, 0.0], "n": nq,
+                      "filled": filled, "layers_seed": 8, "layers": 2, "cluster": 4,
+                      "after_gates": cplx_list(sim.cheat_local()[1]),
+                      "p1": [sim.get_probability([True], [q]) for q in range(nq)]})
+    out["fill"] = fills
+    with open(os.path.join(HERE, "ref_perm_init.json"), "w") as f:
+        json.dump(out, f)
+
+
 def main():
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "perm_init":
+        perm_init_fixture()
+        return
+    perm_init_fixture()
     small = {}
     cases = [("c0_n12_off", 12, 20, "off", 4, 101), ("c0_n12_greedy4", 12, 20, "greedy", 4, 102),
              ("c0_n14_greedy5", 14, 10, "greedy", 5, 103), ("qft10_greedy5", 10, 0, "qft", 5, 104)]

@@ -85,19 +85,17 @@ def test_huge_gate_is_its_own_cluster(hqs):
 
 
 def test_integration_ctypes_stub_runs(hqs, monkeypatch):
-    """The ctypes binding printed for maintainers runs as written: it loads
-    libhqs.so, declares the calls it makes, and turns a failed create (no
-    CUDA device here) into RuntimeError with the library's message."""
-    import re
+    """The ctypes binding printed for maintainers (tests/ctypes_stub.py) runs
+    as written: it loads libhqs.so, declares the calls it makes, and turns a
+    failed create (no CUDA device here) into RuntimeError with the library's
+    message."""
     torch = pytest.importorskip("torch")
     if torch.cuda.is_available():
         pytest.skip("checks the no-device error path")
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     monkeypatch.chdir(root)
-    text = open(os.path.join(root, "INTEGRATION.md")).read()
-    stub = [b for b in re.findall(r"```python\n(.*?)```", text, re.S) if "ctypes.CDLL" in b]
-    assert len(stub) == 1
     ns = {}
-    exec(stub[0], ns)
+    with open(os.path.join(root, "tests", "ctypes_stub.py")) as f:
+        exec(compile(f.read(), "ctypes_stub.py", "exec"), ns)
     with pytest.raises(RuntimeError, match="CUDA"):
         ns["SimulatorBackend"](1, 20, 4)

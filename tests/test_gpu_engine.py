@@ -511,3 +511,66 @@ def test_state_dlpack_view_is_zero_copy(hqs, cuda, precision):
     del sim
     gc.collect()
     assert abs(float(t.abs().square().sum()) - 1) < (1e-12 if precision == "c128" else 1e-5)
+
+
+# ------------------------------------------- permutation getters and fill value
+
+def _fixture_perm_init():
+    with open(os.path.join(GOLDEN, "ref_perm_init.json")) as f:
+        return json.load(f)
+
+
+def _cplx(pairs):
+    return np.array([complex(a, b) for a, b in pairs], dtype=np.complex128)
+
+
+def test_set_qubits_perm_relabels_like_reference(make):
+    """SetQubitsPermutation relabels positions without moving data and the
+    getters return locals_ ++ globals_ (SimulatorMPI.cpp:652-679): ids, local
+    and global ids before and after the relabelling, then the state, P(q=1),
+    amplitudes and a joint probability as the reference returned them."""
+    from hiqsimulator_gb300 import circuits
+    fx = _fixture_perm_init()["perm"]
+    n = fx["n"]
+    gates = circuits.random_layers(fx["seed"], list(range(n)), fx["layers"])
+    cmds = circuits.greedy_stream(gates, list(range(n)), fx["cluster"])
+    sim = make(seed=fx["seed"], cluster=fx["cluster"])
+    sim.allocate_qureg(fx["alloc_ids"], 0)
+    circuits.replay(sim, cmds)
+    sim.run()
+    assert list(sim.get_qubits_ids()) == fx["before"]["ids"]
+    assert list(sim.get_local_qubits_ids()) == fx["before"]["local"]
+    assert list(sim.get_global_qubits_ids()) == fx["before"]["global"]
+    sim.set_qubits_perm(fx["perm"])
+    assert list(sim.get_qubits_ids()) == fx["after"]["ids"]
+    assert list(sim.get_local_qubits_ids()) == fx["after"]["local"]
+    assert list(sim.get_global_qubits_ids()) == fx["after"]["global"]
+    id2pos, vec = sim.cheat_local()
+    assert {str(k): int(v) for k, v in id2pos.items()} == fx["id2pos"]
+    assert np.max(np.abs(np.asarray(vec) - _cplx(fx["state"]))) < TOL
+    for q in range(n):
+        assert abs(sim.get_probability([True], [q]) - fx["p1"][q]) < TOL
+    for bits, want in zip(fx["amp_bits"], _cplx(fx["amps"])):
+        assert abs(sim.get_amplitude(bits, fx["amp_ids"]) - want) < TOL
+    assert abs(sim.get_probability([True, False], [4, 1]) - fx["p_pair"]) < TOL
+
+
+@pytest.mark.parametrize("case", [0, 1, 2])
+def test_allocate_qureg_fill_value_like_reference(make, case):
+    """AllocateQureg(ids, init != 0) fills every amplitude with init
+    (SimulatorMPI.cpp:218-251, FillVector); the filled state, then the state
+    and P(q=1) after a few greedy-fused random layers."""
+    from hiqsimulator_gb300 import circuits
+    fx = _fixture_perm_init()["fill"][case]
+    nq = fx["n"]
+    sim = make(seed=7, cluster=fx["cluster"])
+    sim.allocate_qureg(list(range(nq)), complex(*fx["init"]))
+    _, vec = sim.cheat_local()
+    assert np.max(np.abs(np.asarray(vec) - _cplx(fx["filled"]))) == 0.0
+    g = circuits.random_layers(fx["layers_seed"], list(range(nq)), fx["layers"])
+    circuits.replay(sim, circuits.greedy_stream(g, list(range(nq)), fx["cluster"]))
+    sim.run()
+    _, vec = sim.cheat_local()
+    assert np.max(np.abs(np.asarray(vec) - _cplx(fx["after_gates"]))) < TOL
+    for q in range(nq):
+        assert abs(sim.get_probability([True], [q]) - fx["p1"][q]) < TOL

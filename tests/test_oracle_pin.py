@@ -189,3 +189,33 @@ def test_oracle_matches_release_build_when_present(tmp_path):
     gates = circuits.qft(qs) + circuits.random_layers(13, qs, 4)
     o = _run_oracle(n, circuits.greedy_stream(gates, qs, 4), 3, 4)
     assert np.max(np.abs(np.load(out) - o.vec)) < TOL
+
+
+def test_oracle_matches_reference_perm_and_fill():
+    """The oracle's set_qubits_perm relabelling, qubit-id getters and
+    allocate_qureg fill value against ref_perm_init.json."""
+    fx = json.load(open(os.path.join(GOLDEN, "ref_perm_init.json")))
+    p = fx["perm"]
+    n = p["n"]
+    gates = circuits.random_layers(p["seed"], list(range(n)), p["layers"])
+    sim = OracleSimulator(p["seed"], 24, p["cluster"])
+    sim.allocate_qureg(p["alloc_ids"], 0)
+    circuits.replay(sim, _stream(gates, n, "greedy", p["cluster"]))
+    sim.run()
+    assert list(sim.get_qubits_ids()) == p["before"]["ids"]
+    sim.set_qubits_perm(p["perm"])
+    assert list(sim.get_qubits_ids()) == p["after"]["ids"]
+    id2pos, vec = sim.cheat_local()
+    assert {str(k): int(v) for k, v in id2pos.items()} == p["id2pos"]
+    assert np.max(np.abs(np.asarray(vec) - np.array([complex(*v) for v in p["state"]]))) < TOL
+    for bits, want in zip(p["amp_bits"], p["amps"]):
+        assert abs(sim.get_amplitude(bits, p["amp_ids"]) - complex(*want)) < TOL
+    for f in fx["fill"]:
+        nq = f["n"]
+        sim = OracleSimulator(7, 24, f["cluster"])
+        sim.allocate_qureg(list(range(nq)), complex(*f["init"]))
+        assert np.max(np.abs(sim.vec - np.array([complex(*v) for v in f["filled"]]))) == 0.0
+        g = circuits.random_layers(f["layers_seed"], list(range(nq)), f["layers"])
+        circuits.replay(sim, _stream(g, nq, "greedy", f["cluster"]))
+        sim.run()
+        assert np.max(np.abs(sim.vec - np.array([complex(*v) for v in f["after_gates"]]))) < TOL
