@@ -19,9 +19,9 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-CU_SOURCES = ["kernels.cu", "noalloc.cu"]
+CU_SOURCES = ["kernels.cu", "umma_pass.cu", "noalloc.cu"]
 CXX_SOURCES = ["fusion.cpp", "workspace.cpp", "engine.cpp", "scheduler.cpp", "server.cpp", "capi.cpp"]
-HEADERS = ["hqs_desc.h", "hqs_kernels.h", "hqs_arith.cuh", "fusion.h", "workspace.h", "engine.h", "server.h"]
+HEADERS = ["hqs_desc.h", "hqs_kernels.h", "hqs_arith.cuh", "hqs_tc05.cuh", "fusion.h", "workspace.h", "engine.h", "server.h"]
 
 LIB = os.path.join(PKG, "libhqs.so")
 EXT = sysconfig.get_config_var("EXT_SUFFIX") or ".so"

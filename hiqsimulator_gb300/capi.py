@@ -88,6 +88,8 @@ def load():
     lib.hqs_ws_synchronize.argtypes = [_vp]
     lib.hqs_ws_timer_start.argtypes = [_vp]
     lib.hqs_ws_timer_stop.argtypes = [_vp, _P(ctypes.c_float)]
+    lib.hqs_plan_launches.argtypes = [_i, _i, _i, _P(_i), _P(_i), _P(_u64), _P(_i), _i, _i, _P(LaunchInfo), _sz,
+                                      _P(_sz)]
     lib.hqs_plan_passes.argtypes = [_i, _i, _i, _P(_i), _P(_i), _P(_u64), _P(_i), _i, _i, _P(PassInfo), _sz,
                                     _P(_sz)]
     _lib = lib
@@ -99,6 +101,35 @@ class PassInfo(ctypes.Structure):
                 ("w", ctypes.c_uint32), ("prefetch", ctypes.c_uint32), ("tc_ops", ctypes.c_uint32),
                 ("tile_mask", ctypes.c_uint64), ("fixed_mask", ctypes.c_uint64), ("smem_bytes", ctypes.c_uint64),
                 ("pool_bytes", ctypes.c_uint64), ("sweep_bytes", ctypes.c_uint64)]
+
+
+class LaunchInfo(ctypes.Structure):
+    _fields_ = [("first_op", ctypes.c_uint32), ("nops", ctypes.c_uint32), ("umma", ctypes.c_uint32),
+                ("tc_op", ctypes.c_uint32), ("tile_mask", ctypes.c_uint64), ("target_mask", ctypes.c_uint64),
+                ("fixed_mask", ctypes.c_uint64), ("rank", ctypes.c_uint32), ("nextra", ctypes.c_uint32),
+                ("box_bytes", ctypes.c_uint32), ("dim_kind", ctypes.c_int32 * 5), ("dim_pos", ctypes.c_int32 * 5),
+                ("dim_bits", ctypes.c_int32 * 5), ("pool_bytes", ctypes.c_uint64), ("sweep_bytes", ctypes.c_uint64)]
+
+
+def plan_launches(n, arith, gates, max_tile_bits=0, max_ops=0):
+    """The launches the engine makes for gates (k, positions, ctrl_mask,
+    diag[, matrix]), computed on the host: a list of dicts (LaunchInfo
+    fields, arrays as lists)."""
+    lib = load()
+    nops, k, pos, ctrl, diag = _gate_arrays(gates)
+    cap = max(nops, 1)
+    out = (LaunchInfo * cap)()
+    nl = _sz()
+    check_ws(lib.hqs_plan_launches(n, ARITH[arith], nops, _ptr(k, _i), _ptr(pos, _i), _ptr(ctrl, _u64),
+                                   _ptr(diag, _i), max_tile_bits, max_ops, out, cap, ctypes.byref(nl)))
+    res = []
+    for i in range(nl.value):
+        d = {}
+        for f, _ in LaunchInfo._fields_:
+            v = getattr(out[i], f)
+            d[f] = list(v) if f.startswith("dim_") else v
+        res.append(d)
+    return res
 
 
 def _gate_arrays(gates):

@@ -636,6 +636,46 @@ int hqs_plan_passes(int n, int arith, int nops, const int* k, const int* pos, co
     });
 }
 
+int hqs_plan_launches(int n, int arith, int nops, const int* k, const int* pos, const uint64_t* ctrl, const int* diag,
+                      int max_tile_bits, int max_ops, hqs_launch_info* out, size_t cap, size_t* nlaunches) {
+    return guarded(g_err, [&]() {
+        need(n >= 1 && n <= 40, "n out of range");
+        need(arith >= HQS_ARITH_F64 && arith <= HQS_ARITH_TC64, "unknown arithmetic");
+        need(nops >= 0 && (nops == 0 || (k && pos && ctrl && diag)), "null gate arrays");
+        need(nlaunches && (cap == 0 || out), "null output");
+        std::vector<hqs::GateOp> ops = ops_from_arrays(n, nops, k, pos, ctrl, diag, nullptr);
+        for (auto& op : ops) op.m.resize(op.diag ? ((size_t)1 << op.k) : op.k == 0 ? 1 : ((size_t)1 << (2 * op.k)));
+        const std::vector<hqs::LaunchPlan> L = hqs::plan_launches(
+            n, arith, ops, max_tile_bits > 0 ? max_tile_bits : 11, max_ops > 0 ? max_ops : 16, hqs::umma_enabled());
+        *nlaunches = L.size();
+        for (size_t i = 0; i < L.size() && i < cap; ++i) {
+            hqs_launch_info& o = out[i];
+            std::memset(&o, 0, sizeof(o));
+            const hqs::PassDesc& d = L[i].umma ? L[i].udesc.d : L[i].pass.desc;
+            o.first_op = (uint32_t)L[i].first;
+            o.nops = (uint32_t)d.nops;
+            o.umma = L[i].umma ? 1u : 0u;
+            for (int b = 0; b < d.q; ++b) o.tile_mask |= 1ULL << d.tile_pos[b];
+            o.fixed_mask = d.fixed_mask;
+            o.pool_bytes = L[i].pool_bytes;
+            o.sweep_bytes = L[i].bytes;
+            if (L[i].umma) {
+                const hqs::UmmaDesc& u = L[i].udesc;
+                o.tc_op = (uint32_t)u.tc_op;
+                for (int j = 0; j < 5; ++j) o.target_mask |= 1ULL << d.tile_pos[u.tslot[j]];
+                o.rank = u.rank;
+                o.nextra = u.nextra;
+                o.box_bytes = u.box_bytes;
+                for (int j = 0; j < 5; ++j) {
+                    o.dim_kind[j] = j < u.rank ? u.dim_kind[j] : -1;
+                    o.dim_pos[j] = u.dim_pos[j];
+                    o.dim_bits[j] = u.dim_bits[j];
+                }
+            }
+        }
+    });
+}
+
 int hqs_apply_gates(hqs_ws* ws, void* state, int n, int arith, int nops, const int* k, const int* pos,
                     const uint64_t* ctrl, const int* diag, const double* mats, int max_tile_bits, int max_ops,
                     uint64_t* bytes_out, uint64_t* passes_out) {
@@ -705,7 +745,7 @@ int hqs_drop_bit(hqs_ws* ws, void* state, int n, int arith, int pos, int keep) {
 }
 
 int hqs_ws_synchronize(hqs_ws* ws) {
-    WS_CALL(ws, hqs::cuda_check(cudaStreamSynchronize(ws->ws->stream()), "cudaStreamSynchronize"));
+    WS_CALL(ws, ws->ws->synchronize_checked());
 }
 
 int hqs_ws_timer_start(hqs_ws* ws) {

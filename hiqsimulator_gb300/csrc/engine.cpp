@@ -86,7 +86,7 @@ void Engine::flush() {
 
 void Engine::synchronize() {
     flush();
-    cuda_check(cudaStreamSynchronize(ws_.stream()), "cudaStreamSynchronize");
+    ws_.synchronize_checked();
 }
 
 void Engine::ensure_capacity(uint64_t amps) {

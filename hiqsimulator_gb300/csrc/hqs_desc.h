@@ -71,6 +71,36 @@ struct PassDesc {
     OpDesc ops[kMaxOpsPerPass];
 };
 
+// Tensor-memory pass (complex128): one dense gate on the tcgen05 tensor cores
+// plus runs of diagonal / scalar gates before and after it, over tiles of
+// 2^12 amplitudes: five target positions (gates on fewer qubits are widened
+// with identity factors) and 128 index groups, the MMA's M. Every real is
+// written as six balanced base-2^9 digits; the tile's tensor-memory
+// accumulators hold the six digit levels of each output.
+constexpr int kUmmaTileBits = 12;
+constexpr int kUmmaGroups = 128;
+constexpr int kUmmaDigits = 6;
+constexpr uint32_t kUmmaGatePlaneBytes = 6 * 64 * 128;           // six gate digit planes, 64 rows x 128 B
+constexpr uint32_t kUmmaGateBytes = kUmmaGatePlaneBytes + 64 * 4;  // + column exponents
+constexpr uint32_t kUmmaEwMaxBytes = 12 * 1024;                    // element-wise matrices staged per pass
+
+struct UmmaDesc {
+    PassDesc d;            // tile (q = 12), fixed mask, ops; ops[tc_op] is the dense gate
+    int32_t tc_op;
+    uint32_t gate_off;     // byte offset of the gate block in the pool (1024-aligned)
+    uint32_t ew_bytes;     // bytes of element-wise matrices at the start of the pool
+    uint32_t box_bytes;    // bytes of one TMA box; a tile is 2^nextra boxes
+    uint8_t tslot[5];      // tile slots of the five targets, ascending (element bits 0..4)
+    uint8_t rank;          // tensor-map rank (1..5)
+    uint8_t nextra;        // tile bits above the box (one copy per combination)
+    uint8_t pad0;
+    int8_t dim_kind[5];    // 0: inside the box (coordinate 0); 1: gap (from the tile base);
+                           // 2: rest (tile base plus the copy's extra bits)
+    int8_t dim_pos[5];     // first state position of each dimension
+    int8_t dim_bits[5];    // state positions each dimension spans
+    int8_t extra_pos[kMaxTileBits];  // state positions of the extra tile bits, ascending
+};
+
 // true when any op of the pass runs on the tensor cores
 inline bool pass_has_tc(const PassDesc& d) {
     for (int o = 0; o < d.nops; ++o)

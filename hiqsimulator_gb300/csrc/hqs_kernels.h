@@ -28,6 +28,16 @@ size_t pass_smem_bytes(int arith, const PassDesc& d);
 // register budget); shared memory may allow fewer.
 int pass_reg_ctas(int arith, const PassDesc& d);
 
+// Tensor-memory pass over a complex128 state (umma_pass.cu): the pass's
+// element-wise matrices (double-float, at the start of mats) and the dense
+// gate's digit block (at u.gate_off). The TMA tensor map is built from the
+// descriptor and the state pointer.
+cudaError_t launch_umma_pass(void* state, const void* mats, const UmmaDesc& u, cudaStream_t s);
+size_t umma_smem_bytes();
+// Whether a tensor-memory pass on the current device ran out of a bounded
+// wait since the last call (the error word is cleared).
+cudaError_t umma_check_error(bool* failed);
+
 // One entry of a batched launch: a pass over one state. Device-resident.
 struct BatchItem {
     void* state;

@@ -1,0 +1,619 @@
+// Tensor-memory fused pass for complex128 states on sm_103a: one dense
+// k-qubit gate (k <= 5, widened to five targets with identity factors) on the
+// tcgen05 tensor cores, plus the runs of diagonal and scalar gates before and
+// after it, in one sweep over the state. Replaces, for its pass, the
+// reference's kernelK sweep (src/simulator-mpi/kernels/nointrin/kernel5.hpp:
+// 1134-1193) and the diagonal sweeps (kernels_diag.hpp:20-81).
+//
+// Tile: 4096 amplitudes = 128 index groups x 32 inputs (the five target bits).
+// Per tile the gate is the real GEMM Y[128 x 64] = X[128 x 64] B[64 x 64]
+// (interleaved re/im of each group's inputs and outputs). Every state real
+// is written as six balanced base-2^9 digits relative to its group's largest
+// exponent (X' = x 2^(8 - E), |X'| < 2^8), every gate real as six digits
+// relative to its column's largest exponent (B' = b 2^(7 - E_c), |B'| < 2^7,
+// top digit <= 128). Digits are exact in fp16, and the digit products with
+// i + j = L are summed into one fp32 accumulator region per level L = 0..5:
+// levels 0-3 stay below 2^24 (exact integers), levels 4-5 carry at most a
+// few units of rounding (2^-46 of the row scale). Dropped levels >= 6 are
+// below 2^-45 of the row scale for any inputs.
+//
+// Operands: the state digit planes are MMA operand A (M = 128 groups, K = 64
+// reals), planes 0-3 in tensor memory and planes 4-5 in shared memory (128B
+// swizzle); the gate's six digit planes are operand B (N = 64 outputs per
+// digit, shared memory). X_i times the gate planes j = 0..5-i, placed side by
+// side along N, accumulates each (i, j) product directly into the region of
+// level i + j: one MMA covers up to four levels (N = 256).
+//
+// Warps: 0-7 split digits and assemble outputs (CUDA cores), warp 8 moves
+// tiles with TMA tensor copies (load into one of two tile buffers, store back
+// from it), warp 9 allocates tensor memory and issues the MMAs. Every wait is
+// bounded; a wait that runs out raises a CTA-wide abort flag, every warp
+// leaves its loop, the TMA warp waits (bounded) for its copies in flight, the
+// MMA warp for its MMAs, tensor memory is freed and the host sees the error
+// word.
+#include <cuda.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "hqs_arith.cuh"
+#include "hqs_kernels.h"
+#include "hqs_tc05.cuh"
+
+namespace hqs {
+
+namespace {
+
+using namespace tc05;
+
+constexpr int kCompute = 256;  // warps 0..7
+constexpr int kTmaWarp = 8, kMmaWarp = 9;
+constexpr int kThreadsU = 320;
+
+// shared memory, relative to a 1024-byte aligned base
+constexpr uint32_t kSmGate = 0;             // 6 gate digit planes, 64 rows x 128 B each
+constexpr uint32_t kSmPlanes = 49152;       // state digit planes 4 and 5, 128 rows x 128 B each
+constexpr uint32_t kSmTile0 = 81920;        // tile buffers, 4096 x double2
+constexpr uint32_t kSmTile1 = 147456;
+constexpr uint32_t kSmEcol = 212992;        // int[64]: gate column exponents
+constexpr uint32_t kSmErow = kSmEcol + 256; // int[128]: group exponents of the current tile
+constexpr uint32_t kSmMx = kSmErow + 512;   // uint32[256]: half-group maxima
+constexpr uint32_t kSmGb = kSmMx + 1024;    // uint16[128]: tile index of each group's input 0
+constexpr uint32_t kSmOff = kSmGb + 256;    // uint16[32]: tile offset of each input
+constexpr uint32_t kSmBar = kSmOff + 64;    // 6 mbarriers
+constexpr uint32_t kSmMisc = kSmBar + 64;   // tensor-memory base, abort flag
+constexpr uint32_t kSmEw = kSmMisc + 64;    // element-wise matrices (float4)
+constexpr uint32_t kSmBytes = kSmEw + kUmmaEwMaxBytes + 1024;  // + alignment slack
+
+// tensor-memory columns: six level regions of 64, then state planes 0-3
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kTmPlanes = 384;
+
+constexpr uint32_t kTileBytes = 4096 * 16;
+
+__device__ __forceinline__ uint64_t insert_zero_u(uint64_t v, int p) {
+    const uint64_t low = v & ((1ULL << p) - 1ULL);
+    return ((v - low) << 1) | low;
+}
+
+// First state index of tile t and the walk to the CTA's next tile (the
+// tile's bits deposited over the positions outside the tile and the fixed
+// positions; fixed positions set).
+struct Walk {
+    uint64_t spread, step, base, fixed;
+    __device__ Walk(const PassDesc& d, uint64_t t0, uint64_t stride) {
+        uint64_t ins = 0;
+        for (int i = 0; i < d.nins; ++i) ins |= 1ULL << d.ins_pos[i];
+        spread = ~ins & (d.n >= 64 ? ~0ULL : ((1ULL << d.n) - 1ULL));
+        fixed = d.fixed_mask;
+        base = deposit(d, t0) | fixed;
+        step = deposit(d, stride);
+    }
+    __device__ static uint64_t deposit(const PassDesc& d, uint64_t t) {
+        for (int i = 0; i < d.nins; ++i) t = insert_zero_u(t, d.ins_pos[i]);
+        return t;
+    }
+    __device__ uint64_t after(uint64_t b) const { return ((((b & spread) | ~spread) + step) & spread) | fixed; }
+};
+
+// TMA box coordinates of copy c of the tile with base index b
+__device__ __forceinline__ void tile_coords(const UmmaDesc& u, uint64_t b, uint32_t c, int32_t (&co)[5]) {
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        int32_t v = 0;
+        if (i < u.rank) {
+            if (u.dim_kind[i] == 1) {
+                v = (int32_t)((b >> u.dim_pos[i]) & ((1ULL << u.dim_bits[i]) - 1ULL));
+            } else if (u.dim_kind[i] == 2) {
+                uint64_t r = b >> u.dim_pos[i];
+                for (int k = 0; k < u.nextra; ++k)
+                    if ((c >> k) & 1u) r |= 1ULL << (u.extra_pos[k] - u.dim_pos[i]);
+                v = (int32_t)r;
+            }
+        }
+        co[i] = v;
+    }
+}
+
+// ------------------------------------------------------------------ digits
+constexpr float kMagic0 = 12582912.0f;  // 1.5 * 2^23: rounds to integers
+constexpr float kMagic9 = 24576.0f;     // 1.5 * 2^14: rounds to multiples of 2^-9
+constexpr float kMagic27 = 0.09375f;    // 1.5 * 2^-4: rounds to multiples of 2^-27
+
+__device__ __forceinline__ float rnd_with(float x, float m) { return __fsub_rn(__fadd_rn(x, m), m); }
+
+// The six balanced base-2^9 digits of X' = v 2^(1030 - Eb) (|X'| < 2^8 for
+// every v of the group): X' = sum_i d_i 2^(-9 i) up to 2^-40 (2^-48 of the
+// group's scale). X' = H + L splits the double's 53-bit significand into its
+// top 24 bits (H) and the remaining 29 bits (L, rounded to 24 bits).
+// T0 = H rounded to multiples of 2^-9 carries digits 0-1, T1 (multiples of
+// 2^-27) digits 2-3, T2 = the rest digits 4-5. |d_i| <= 256 except d_2,
+// whose bound is 260 (H's rounding tie at 2^-10 ignores L, |L| < 2^-16).
+__device__ __forceinline__ void digits6(double v, int Eb, float (&dg)[6]) {
+    const uint32_t hi = (uint32_t)__double2hiint(v), lo = (uint32_t)__double2loint(v);
+    const int eb = (int)((hi >> 20) & 0x7FFu);
+    int dH = eb - Eb + 134;
+    dH = eb == 0 ? 0 : max(dH, 0);
+    const uint32_t sgn = hi & 0x80000000u;
+    const uint32_t mant = __funnelshift_l(lo, hi, 3);
+    const float H = __uint_as_float((mant & 0x7FFFFFu) | ((uint32_t)dH << 23) | sgn);
+    const int dL = max(dH - 52, 0);
+    const float L = __fmul_rn(__uint2float_rn(lo & 0x1FFFFFFFu), __uint_as_float(((uint32_t)dL << 23) | sgn));
+    const float T0 = rnd_with(H, kMagic9);
+    const float R0 = __fsub_rn(H, T0);
+    const float R27 = rnd_with(R0, kMagic27);
+    const float D = __fadd_rn(__fsub_rn(R0, R27), L);
+    const float D27 = rnd_with(D, kMagic27);
+    const float T1 = __fadd_rn(R27, D27);
+    const float T2 = __fsub_rn(D, D27);
+    dg[0] = rnd_with(T0, kMagic0);
+    dg[1] = __fmul_rn(__fsub_rn(T0, dg[0]), 512.f);
+    const float u2 = __fmul_rn(T1, 262144.f);
+    dg[2] = rnd_with(u2, kMagic0);
+    dg[3] = __fmul_rn(__fsub_rn(u2, dg[2]), 512.f);
+    const float u4 = __fmul_rn(T2, 68719476736.f);
+    dg[4] = rnd_with(u4, kMagic0);
+    dg[5] = rnd_with(__fmul_rn(__fsub_rn(u4, dg[4]), 512.f), kMagic0);
+}
+
+__device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
+    __half2 h = __floats2half2_rn(lo, hi);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+// ------------------------------------------------------------------ epilogue
+__device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    e = __fsub_rn(b, __fsub_rn(s, a));
+}
+
+// Output real from the six level sums: V = sum_L S_L 2^(-9 L) (level sums
+// 0-3 exact integers below 2^24, 4-5 within a few units), as a double-float
+// (h, l) by three exact fast two-sums (every partial sum lies on a grid that
+// keeps them exact), then the double h + l times 2^off assembled with
+// integer operations.
+__device__ __forceinline__ double level_sum_to_double(const float (&S)[6], int off) {
+    const float b1 = __fmul_rn(S[1], 1.0f / 512.f);
+    const float b2 = __fmul_rn(S[2], 1.0f / 262144.f);
+    const float b3 = __fmul_rn(S[3], 1.0f / 134217728.f);
+    const float f = __fmaf_rn(S[5], 2.8421709430404007e-14f /* 2^-45 */,
+                              __fmul_rn(S[4], 1.4551915228366852e-11f /* 2^-36 */));
+    float s1, e1, s2, e2, s3, e3;
+    fast_two_sum(S[0], b1, s1, e1);
+    fast_two_sum(s1, b2, s2, e2);
+    fast_two_sum(s2, b3, s3, e3);
+    const float t = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(e3, f));
+    float h, l;
+    fast_two_sum(s3, t, h, l);
+    const uint32_t hb = __float_as_uint(h);
+    const int eh = (int)((hb >> 23) & 0xFFu);
+    const int be = eh + 896 + off;
+    if (eh == 0 || be <= 0) return 0.0;
+    const uint32_t sg = hb & 0x80000000u;
+    const uint32_t whi = ((uint32_t)be << 20) | ((hb & 0x7FFFFFu) >> 3) | sg;
+    const uint32_t wlo = hb << 29;
+    // l in units of the double's last place (2^(eh - 179)), with h's sign;
+    // when h is a power of two and l points toward zero, the result lies in
+    // the binade below, whose last place is half as large
+    const uint32_t lb = __float_as_uint(l);
+    const int below = ((hb & 0x7FFFFFu) == 0u && l != 0.f && ((lb ^ hb) & 0x80000000u)) ? 1 : 0;
+    const int se = min(306 - eh + below, 254);
+    const int delta = __float2int_rn(__fmul_rn(l, __uint_as_float(((uint32_t)se << 23) | sg)));
+    unsigned long long w = ((unsigned long long)whi << 32) | wlo;
+    // magnitude bits plus the signed correction, sign bit kept
+    w = (w & 0x7FFFFFFFFFFFFFFFULL) + (unsigned long long)(long long)delta;
+    w |= (unsigned long long)sg << 32;
+    return __longlong_as_double((long long)w);
+}
+
+// ------------------------------------------------------------------ element-wise runs
+// ops [o0, o1) of the pass (diagonal / scalar), in place on the tile, by the
+// compute threads
+__device__ __forceinline__ void ew_run(double2* buf, const float4* __restrict__ pool, const PassDesc& d, int o0,
+                                       int o1, uint64_t base) {
+    for (int L = threadIdx.x; L < 4096; L += kCompute) {
+        float4 x = ArithDFRaw::elem_load(buf[L]);
+        for (int o = o0; o < o1; ++o) {
+            const OpDesc& op = d.ops[o];
+            if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
+            if (op.k == 0) {
+                x = ArithDFRaw::elem_mul(pool[op.mat_off], x);
+                continue;
+            }
+            if (((uint32_t)L & op.ctrl_local) != op.ctrl_local) continue;
+            int r = 0;
+            for (int j = 0; j < op.k; ++j) {
+                const int sl = op.tslot[j];
+                const uint64_t bit = (sl & kOuterSlot) ? (base >> (sl & 63)) : ((uint64_t)L >> sl);
+                r |= (int)(bit & 1ULL) << j;
+            }
+            x = ArithDFRaw::elem_mul(pool[op.mat_off + r], x);
+        }
+        buf[L] = ArithDFRaw::elem_store(x);
+    }
+}
+
+// ------------------------------------------------------------------ kernel
+__global__ void __launch_bounds__(kThreadsU, 1)
+    umma_pass_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ UmmaDesc u,
+                     const unsigned char* __restrict__ pool, int* __restrict__ err) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+    const PassDesc& d = u.d;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kSmBar);
+    uint64_t* full = bars;        // [2] tile loaded
+    uint64_t* tdone = bars + 2;   // [2] tile computed
+    uint64_t* pbar = bars + 4;    // state digits written
+    uint64_t* mbar = bars + 5;    // MMAs complete
+    uint32_t* tmem_s = reinterpret_cast<uint32_t*>(sm + kSmMisc);
+    volatile int* abort = reinterpret_cast<volatile int*>(sm + kSmMisc + 8);
+    int* erow = reinterpret_cast<int*>(sm + kSmErow);
+    const int* ecol = reinterpret_cast<const int*>(sm + kSmEcol);
+    uint32_t* mxs = reinterpret_cast<uint32_t*>(sm + kSmMx);
+    uint16_t* gb = reinterpret_cast<uint16_t*>(sm + kSmGb);
+    uint16_t* offt = reinterpret_cast<uint16_t*>(sm + kSmOff);
+    const float4* ewp = reinterpret_cast<const float4*>(sm + kSmEw);
+
+    const uint64_t ntiles = 1ULL << (d.n - d.nins);
+    const uint64_t my_n = (uint64_t)blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
+
+    // ---- set-up
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < 6; ++i) mbar_init(&bars[i], 1);
+        *abort = 0;
+        mbar_init_fence();
+    }
+    if (warp == kMmaWarp) tmem_alloc(tmem_s, kTmemCols);
+    if (threadIdx.x < kCompute) {
+        const uint4* gsrc = reinterpret_cast<const uint4*>(pool + u.gate_off);
+        uint4* gdst = reinterpret_cast<uint4*>(sm + kSmGate);
+        for (int i = threadIdx.x; i < (int)(kUmmaGatePlaneBytes / 16); i += kCompute) gdst[i] = gsrc[i];
+        if (threadIdx.x < 64)
+            reinterpret_cast<int*>(sm + kSmEcol)[threadIdx.x] =
+                reinterpret_cast<const int*>(pool + u.gate_off + kUmmaGatePlaneBytes)[threadIdx.x];
+        const uint4* esrc = reinterpret_cast<const uint4*>(pool);
+        uint4* edst = reinterpret_cast<uint4*>(sm + kSmEw);
+        for (int i = threadIdx.x; i < (int)(u.ew_bytes / 16); i += kCompute) edst[i] = esrc[i];
+        // group g's first tile index: g's bits deposited over the slots that
+        // are not targets; input e's offset: e's bits over the target slots
+        uint32_t tmask = 0;
+        for (int j = 0; j < 5; ++j) tmask |= 1u << u.tslot[j];
+        if (threadIdx.x < 128) {
+            uint32_t v = 0, g = threadIdx.x;
+            for (int s = 0; s < 12; ++s)
+                if (!((tmask >> s) & 1u)) {
+                    v |= (g & 1u) << s;
+                    g >>= 1;
+                }
+            gb[threadIdx.x] = (uint16_t)v;
+        } else if (threadIdx.x < 160) {
+            const uint32_t e = threadIdx.x - 128;
+            uint32_t v = 0;
+            for (int j = 0; j < 5; ++j) v |= ((e >> j) & 1u) << u.tslot[j];
+            offt[e] = (uint16_t)v;
+        }
+    }
+    fence_proxy_async();
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    const uint32_t tmem = *tmem_s;
+
+    if (warp == kTmaWarp) {
+        // ---- tile loads and stores
+        const uint32_t ncopy = 1u << u.nextra;
+        uint32_t issued[2] = {0, 0};
+        auto load = [&](uint64_t b, int s) {
+            unsigned char* buf = sm + (s ? kSmTile1 : kSmTile0);
+            if (lane == 0) {
+                mbar_arrive_expect_tx(&full[s], kTileBytes);
+                for (uint32_t c = 0; c < ncopy; ++c) {
+                    int32_t co[5];
+                    tile_coords(u, b, c, co);
+                    tma_load(buf + (size_t)c * u.box_bytes, &tmap, co, u.rank, &full[s]);
+                }
+            }
+            ++issued[s];
+        };
+        const Walk walk(d, blockIdx.x, gridDim.x);
+        uint64_t lb = walk.base;  // base of the next tile to load
+        if (my_n > 0) {
+            load(lb, 0);
+            lb = walk.after(lb);
+        }
+        if (my_n > 1) {
+            load(lb, 1);
+            lb = walk.after(lb);
+        }
+        uint64_t sb = walk.base;  // base of the next tile to store
+        for (uint64_t it = 0; it < my_n; ++it) {
+            const int s = (int)(it & 1);
+            bool ok = true;
+            if (lane == 0) ok = mbar_wait(&tdone[s], (uint32_t)((it >> 1) & 1), abort);
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
+            if (lane == 0) {
+                const unsigned char* buf = sm + (s ? kSmTile1 : kSmTile0);
+                for (uint32_t c = 0; c < ncopy; ++c) {
+                    int32_t co[5];
+                    tile_coords(u, sb, c, co);
+                    tma_store(&tmap, co, u.rank, buf + (size_t)c * u.box_bytes);
+                }
+                bulk_commit();
+                bulk_wait_read0();
+            }
+            __syncwarp();
+            sb = walk.after(sb);
+            if (it + 2 < my_n) {
+                load(lb, s);
+                lb = walk.after(lb);
+            }
+        }
+        if (lane == 0) {
+            bulk_wait0();
+            // loads still in flight (a loop left early): wait for them before
+            // the CTA's shared memory goes away
+            for (int s = 0; s < 2; ++s)
+                if (issued[s])
+                    for (uint32_t i = 0; i < kWaitLimit && !mbar_try(&full[s], (issued[s] - 1) & 1u); ++i) {
+                    }
+        }
+        __syncwarp();
+    } else if (warp == kMmaWarp) {
+        // ---- MMA issue
+        const uint32_t idesc256 = idesc_f16(128, 256), idesc192 = idesc_f16(128, 192),
+                       idesc128 = idesc_f16(128, 128), idesc64 = idesc_f16(128, 64);
+        const uint32_t gate = smem_u32(sm + kSmGate), planes = smem_u32(sm + kSmPlanes);
+        uint64_t committed = 0;
+        for (uint64_t it = 0; it < my_n; ++it) {
+            bool ok = true;
+            if (lane == 0) ok = mbar_wait(pbar, (uint32_t)(it & 1), abort);
+            ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+            if (!ok) break;
+            fence_after_sync();
+            if (lane == 0) {
+#pragma unroll
+                for (int ks = 0; ks < 4; ++ks) {
+                    // X_i times gate digits j0.. accumulates at level region i + j0
+                    auto gdesc = [&](int j0) { return sdesc_sw128(gate + (uint32_t)j0 * 8192u + (uint32_t)ks * 32u); };
+                    auto ta = [&](int i) { return tmem + kTmPlanes + (uint32_t)i * 32u + (uint32_t)ks * 8u; };
+                    auto td = [&](int lev) { return tmem + (uint32_t)lev * 64u; };
+                    const uint32_t acc0 = ks > 0 ? 1u : 0u;
+                    mma_ts(td(0), ta(0), gdesc(0), idesc256, acc0);  // levels 0-3
+                    mma_ts(td(4), ta(0), gdesc(4), idesc128, acc0);  // levels 4-5
+                    mma_ts(td(1), ta(1), gdesc(0), idesc256, 1u);    // levels 1-4
+                    mma_ts(td(5), ta(1), gdesc(4), idesc64, 1u);     // level 5
+                    mma_ts(td(2), ta(2), gdesc(0), idesc256, 1u);    // levels 2-5
+                    mma_ts(td(3), ta(3), gdesc(0), idesc192, 1u);    // levels 3-5
+                    const uint64_t a4 = sdesc_sw128(planes + (uint32_t)ks * 32u);
+                    const uint64_t a5 = sdesc_sw128(planes + 16384u + (uint32_t)ks * 32u);
+                    mma_ss(td(4), a4, gdesc(0), idesc128, 1u);       // levels 4-5
+                    mma_ss(td(5), a5, gdesc(0), idesc64, 1u);        // level 5
+                }
+                mma_commit(mbar);
+            }
+            __syncwarp();
+            committed = it + 1;
+        }
+        if (committed > 0 && lane == 0) {
+            // the last MMAs must be complete before tensor memory is freed
+            for (uint32_t i = 0; i < kWaitLimit && !mbar_try(mbar, (uint32_t)((committed - 1) & 1)); ++i) {
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---- compute warps: digits, then outputs
+        const int q4 = warp & 3, half = warp >> 2, g = q4 * 32 + lane;
+        const OpDesc& tc = d.ops[u.tc_op];
+        const uint32_t lane_base = (uint32_t)(q4 * 32) << 16;
+        const Walk walk(d, blockIdx.x, gridDim.x);
+        uint64_t base = walk.base;
+        for (uint64_t it = 0; it < my_n; ++it, base = walk.after(base)) {
+            const int s = (int)(it & 1);
+            double2* buf = reinterpret_cast<double2*>(sm + (s ? kSmTile1 : kSmTile0));
+            mbar_wait(&full[s], (uint32_t)((it >> 1) & 1), abort);
+            bar_sync(1, kCompute);
+            if (*abort) break;
+            if (u.tc_op > 0) {
+                ew_run(buf, ewp, d, 0, u.tc_op, base);
+                bar_sync(1, kCompute);
+            }
+            const bool act = (base & tc.ctrl_outer) == tc.ctrl_outer;
+            if (act) {
+                // digit planes of the tile's 128 groups; this thread: group g,
+                // inputs 16 half .. 16 half + 15
+                const uint32_t gbase = gb[g];
+                double2 x[16];
+                uint32_t mx = 0;
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    x[i] = buf[gbase | offt[half * 16 + i]];
+                    mx = max(mx, (uint32_t)__double2hiint(x[i].x) & 0x7FFFFFFFu);
+                    mx = max(mx, (uint32_t)__double2hiint(x[i].y) & 0x7FFFFFFFu);
+                }
+                mxs[threadIdx.x] = mx;
+                bar_sync(1, kCompute);
+                const int Eb = (int)(max(mxs[g], mxs[128 + g]) >> 20);
+                if (half == 0) erow[g] = Eb;
+#pragma unroll
+                for (int bt = 0; bt < 2; ++bt) {
+                    uint32_t pl[6][8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        float dr[6], di[6];
+                        digits6(x[bt * 8 + i].x, Eb, dr);
+                        digits6(x[bt * 8 + i].y, Eb, di);
+#pragma unroll
+                        for (int p = 0; p < 6; ++p) pl[p][i] = pack_h2(dr[p], di[p]);
+                    }
+                    const uint32_t e0 = (uint32_t)(half * 16 + bt * 8);
+#pragma unroll
+                    for (int p = 0; p < 4; ++p) tmem_st8(tmem + lane_base + kTmPlanes + (uint32_t)p * 32u + e0, pl[p]);
+                    const uint32_t c0 = e0 >> 2;
+#pragma unroll
+                    for (int p = 4; p < 6; ++p) {
+                        unsigned char* row = sm + kSmPlanes + (uint32_t)(p - 4) * 16384u + (uint32_t)g * 128u;
+                        *reinterpret_cast<uint4*>(row + ((c0 ^ (g & 7)) << 4)) =
+                            make_uint4(pl[p][0], pl[p][1], pl[p][2], pl[p][3]);
+                        *reinterpret_cast<uint4*>(row + (((c0 + 1) ^ (g & 7)) << 4)) =
+                            make_uint4(pl[p][4], pl[p][5], pl[p][6], pl[p][7]);
+                    }
+                }
+                tmem_st_wait();
+                fence_proxy_async();
+            }
+            fence_before_sync();
+            bar_sync(1, kCompute);
+            if (threadIdx.x == 0) mbar_arrive(pbar);
+            mbar_wait(mbar, (uint32_t)(it & 1), abort);
+            bar_sync(1, kCompute);
+            if (*abort) break;
+            fence_after_sync();
+            if (act && (gb[g] & tc.ctrl_local) == tc.ctrl_local) {
+                // outputs: group g, output reals 32 half .. 32 half + 31
+                const int Eb = erow[g];
+                const uint32_t gbase = gb[g];
+#pragma unroll
+                for (int ch = 0; ch < 4; ++ch) {
+                    const uint32_t n0 = (uint32_t)(half * 32 + ch * 8);
+                    uint32_t r[6][8];
+#pragma unroll
+                    for (int lev = 0; lev < 6; ++lev) tmem_ld8(tmem + lane_base + (uint32_t)lev * 64u + n0, r[lev]);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        double out[2];
+#pragma unroll
+                        for (int p = 0; p < 2; ++p) {
+                            const int c = a * 2 + p;
+                            const float S[6] = {__uint_as_float(r[0][c]), __uint_as_float(r[1][c]),
+                                                __uint_as_float(r[2][c]), __uint_as_float(r[3][c]),
+                                                __uint_as_float(r[4][c]), __uint_as_float(r[5][c])};
+                            out[p] = Eb == 0 ? 0.0 : level_sum_to_double(S, Eb + ecol[n0 + c] - 2059);
+                        }
+                        buf[gbase | offt[(n0 >> 1) + a]] = make_double2(out[0], out[1]);
+                    }
+                }
+            }
+            fence_before_sync();
+            bar_sync(1, kCompute);
+            if (u.tc_op + 1 < d.nops) {
+                ew_run(buf, ewp, d, u.tc_op + 1, d.nops, base);
+                bar_sync(1, kCompute);
+            }
+            fence_proxy_async();
+            bar_sync(1, kCompute);
+            if (threadIdx.x == 0) mbar_arrive(&tdone[s]);
+        }
+    }
+
+    // ---- tear-down
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (warp == kMmaWarp) tmem_dealloc(tmem, kTmemCols);
+    if (threadIdx.x == 0 && *abort) atomicOr(err, 1);
+}
+
+// ------------------------------------------------------------------ host
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    return fn;
+}
+
+constexpr int kMaxDev = 64;
+std::mutex g_umma_mu;
+int* g_err_word[kMaxDev] = {nullptr};
+bool g_attr_set[kMaxDev] = {false};
+
+int current_device() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDev) return -1;
+    return dev;
+}
+
+}  // namespace
+
+size_t umma_smem_bytes() { return kSmBytes; }
+
+cudaError_t launch_umma_pass(void* state, const void* mats, const UmmaDesc& u, cudaStream_t s) {
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return cudaErrorNotSupported;
+    // the state viewed as doubles: each dimension spans dim_bits state
+    // positions from dim_pos (dimension 0 also the re/im pair)
+    cuuint64_t gdim[5], gstr[4];
+    cuuint32_t box[5], es[5];
+    for (int i = 0; i < u.rank; ++i) {
+        gdim[i] = (i == 0 ? 2ULL : 1ULL) << u.dim_bits[i];
+        box[i] = u.dim_kind[i] == 0 ? (cuuint32_t)gdim[i] : 1u;
+        es[i] = 1;
+        if (i > 0) gstr[i - 1] = 16ULL << u.dim_pos[i];
+    }
+    CUtensorMap tm;
+    const CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, (cuuint32_t)u.rank, state, gdim,
+                           u.rank > 1 ? gstr : nullptr, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
+    const int dev = current_device();
+    if (dev < 0) return cudaErrorInvalidDevice;
+    int* err = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_umma_mu);
+        if (!g_err_word[dev]) {
+            cudaError_t e = cudaMalloc(&g_err_word[dev], sizeof(int));
+            if (e != cudaSuccess) return e;
+            e = cudaMemset(g_err_word[dev], 0, sizeof(int));
+            if (e != cudaSuccess) return e;
+        }
+        if (!g_attr_set[dev]) {
+            cudaError_t e =
+                cudaFuncSetAttribute(umma_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmBytes);
+            if (e != cudaSuccess) return e;
+            g_attr_set[dev] = true;
+        }
+        err = g_err_word[dev];
+    }
+    const uint64_t ntiles = 1ULL << (u.d.n - u.d.nins);
+    const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)device_sm_count());
+    umma_pass_kernel<<<grid, kThreadsU, kSmBytes, s>>>(tm, u, static_cast<const unsigned char*>(mats), err);
+    return cudaGetLastError();
+}
+
+cudaError_t umma_check_error(bool* failed) {
+    *failed = false;
+    const int dev = current_device();
+    if (dev < 0) return cudaSuccess;
+    int* err = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_umma_mu);
+        err = g_err_word[dev];
+    }
+    if (!err) return cudaSuccess;
+    int h = 0;
+    cudaError_t e = cudaMemcpy(&h, err, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return e;
+    if (h) {
+        *failed = true;
+        e = cudaMemset(err, 0, sizeof(int));
+    }
+    return e;
+}
+
+}  // namespace hqs

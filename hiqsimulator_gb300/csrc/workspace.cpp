@@ -1,6 +1,7 @@
 #include "workspace.h"
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -34,6 +35,13 @@ Workspace::~Workspace() {
     }
     for (cudaEvent_t e : event_pool_) cudaEventDestroy(e);
     if (stream_) cudaStreamDestroy(stream_);
+}
+
+void Workspace::synchronize_checked() {
+    cuda_check(cudaStreamSynchronize(stream_), "cudaStreamSynchronize");
+    bool failed = false;
+    cuda_check(umma_check_error(&failed), "umma_check_error");
+    if (failed) throw CudaError("tensor-memory pass: a bounded device wait ran out (results of the pass are invalid)");
 }
 
 void* Workspace::scratch(size_t bytes) {
@@ -472,9 +480,362 @@ void write_pass_pool(int arith, const PassDesc& d, const GateOp* ops, unsigned c
     }
 }
 
+// ------------------------------------------------------- tensor-memory passes
+
+bool umma_enabled() {
+    static const bool on = [] {
+        const char* v = std::getenv("HQS_UMMA");
+        return !(v && v[0] == '0');
+    }();
+    return on;
+}
+
+bool umma_candidate(int arith, const GateOp& op) {
+    return arith == kArithTC && !op.diag && op.k >= 3 && op.k <= 5;
+}
+
+static bool elementwise_op(const GateOp& op) { return op.k == 0 || op.diag; }
+
+// double-float matrix entries (16 B each) of an element-wise op
+static size_t ew_pool_bytes(const GateOp& op) { return op.m.size() * 16; }
+
+// The six balanced base-2^9 digits of a gate real v relative to its column's
+// largest biased exponent ebmax, with the column scaled to |v'| < 2^7:
+// a = rint(|v| 2^(1074 - ebmax)) (to nearest, ties to even; a < 2^52) cut
+// into 9-bit fields, balanced into [-256, 255] with carries upward (the top
+// digit ends at most 128), then given v's sign.
+static void gate_digits9(double v, int ebmax, int (&d)[6]) {
+    uint64_t u;
+    std::memcpy(&u, &v, 8);
+    const int eb = (int)((u >> 52) & 0x7FF);
+    uint64_t a = 0;
+    const int sh = ebmax - eb + 1;
+    if (eb != 0 && sh < 62) {
+        const uint64_t M = (u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
+        a = (M + (1ULL << (sh - 1)) - 1ULL + ((M >> sh) & 1ULL)) >> sh;
+    }
+    int r[6];
+    for (int i = 1; i < 6; ++i) r[i] = (int)((a >> (9 * (5 - i))) & 511u);
+    r[0] = (int)(a >> 45);
+    for (int i = 5; i >= 1; --i) {
+        const int c = (r[i] + 256) >> 9;
+        r[i] -= c << 9;
+        r[i - 1] += c;
+    }
+    const bool neg = (u >> 63) != 0;
+    for (int i = 0; i < 6; ++i) d[i] = neg ? -r[i] : r[i];
+}
+
+// Gate block of a tensor-memory pass: the gate widened to the five target
+// positions pos5 (ascending; e bit j <-> pos5[j], identity on the positions
+// that are not the gate's targets), in real form B[k][n] (k = 2c + part of
+// input c, n = 2r + part of output r), as six digit planes (plane j: rows
+// n = 0..63 of 64 fp16 over k, K-major with the 128-byte swizzle of the MMA
+// operand), then the 64 column exponents as int32.
+static void build_umma_gate(const GateOp& g, const int (&pos5)[5], unsigned char* dst) {
+    int realbit[5];
+    for (int j = 0; j < 5; ++j) {
+        realbit[j] = -1;
+        for (int t = 0; t < g.k; ++t)
+            if (g.pos[t] == pos5[j]) realbit[j] = t;
+    }
+    const int D = 1 << g.k;
+    auto u5 = [&](int r5, int c5) -> cplx {
+        int r = 0, c = 0;
+        for (int j = 0; j < 5; ++j) {
+            const int rb = (r5 >> j) & 1, cb = (c5 >> j) & 1;
+            if (realbit[j] < 0) {
+                if (rb != cb) return cplx(0.0, 0.0);
+            } else {
+                r |= rb << realbit[j];
+                c |= cb << realbit[j];
+            }
+        }
+        return g.m[(size_t)r * D + c];
+    };
+    auto bval = [&](int kk, int nn) -> double {
+        const cplx m = u5(nn >> 1, kk >> 1);
+        const int pin = kk & 1, pout = nn & 1;
+        if (pin == 0) return pout == 0 ? m.real() : m.imag();
+        return pout == 0 ? -m.imag() : m.real();
+    };
+    uint16_t* planes = reinterpret_cast<uint16_t*>(dst);
+    std::memset(planes, 0, kUmmaGatePlaneBytes);
+    int32_t* ecol = reinterpret_cast<int32_t*>(dst + kUmmaGatePlaneBytes);
+    for (int nn = 0; nn < 64; ++nn) {
+        int ebmax = 0;
+        for (int kk = 0; kk < 64; ++kk) ebmax = std::max(ebmax, biased_exponent(bval(kk, nn)));
+        ecol[nn] = ebmax;
+        for (int kk = 0; kk < 64; ++kk) {
+            int dg[6];
+            gate_digits9(bval(kk, nn), ebmax, dg);
+            for (int j = 0; j < 6; ++j) {
+                const int row = 64 * j + nn;
+                const size_t byte = (size_t)row * 128 + ((size_t)(((2 * kk) >> 4) ^ (row & 7)) << 4) + ((2 * kk) & 15);
+                planes[byte / 2] = half_of_int(dg[j]);
+            }
+        }
+    }
+}
+
+// Tensor-memory pass over ops [i0, i1) with the dense gate at tc. Tile: the
+// gate's targets, then the lowest other positions up to 12; when the gate has
+// fewer than five targets, the highest of those positions that are not its
+// controls become extra targets with identity factors. Returns false when the
+// pass cannot be formed (state too small, element-wise matrices too large).
+static bool build_umma(int n, const GateOp* ops, size_t i0, size_t tc, size_t i1, UmmaDesc& u, uint64_t& bytes) {
+    const GateOp& g = ops[tc];
+    uint64_t tmask = 0;
+    for (int t = 0; t < g.k; ++t) tmask |= 1ULL << g.pos[t];
+    std::vector<int> picks;
+    for (int b = 0; b < n && (int)picks.size() < kUmmaTileBits - g.k; ++b)
+        if (!((tmask >> b) & 1ULL)) picks.push_back(b);
+    if ((int)picks.size() < kUmmaTileBits - g.k) return false;
+    uint64_t t5 = tmask;
+    int extra_t = 5 - g.k;
+    for (int i = (int)picks.size() - 1; i >= 0 && extra_t > 0; --i)
+        if (!((g.ctrl_mask >> picks[i]) & 1ULL)) {
+            t5 |= 1ULL << picks[i];
+            --extra_t;
+        }
+    if (extra_t > 0) return false;
+    uint64_t tile = tmask;
+    for (int p : picks) tile |= 1ULL << p;
+    size_t ewb = 0;
+    for (size_t o = i0; o < i1; ++o)
+        if (o != tc) ewb += ew_pool_bytes(ops[o]);
+    if (ewb > kUmmaEwMaxBytes || i1 - i0 > (size_t)kMaxOpsPerPass) return false;
+
+    std::memset(&u, 0, sizeof(u));
+    PassDesc& d = u.d;
+    int slot[64];
+    int c = 0;
+    for (int b = 0; b < n; ++b)
+        if ((tile >> b) & 1ULL) {
+            slot[b] = c;
+            d.tile_pos[c++] = (uint8_t)b;
+        }
+    d.n = n;
+    d.q = kUmmaTileBits;
+    d.w = 0;
+    while (d.w < d.q && d.tile_pos[d.w] == d.w) ++d.w;
+    uint64_t fixed = ~0ULL;
+    for (size_t o = i0; o < i1; ++o) fixed &= ops[o].ctrl_mask & ~tile;
+    d.fixed_mask = fixed;
+    const uint64_t ins = tile | fixed;
+    d.nins = 0;
+    for (int b = 0; b < 64; ++b)
+        if ((ins >> b) & 1ULL) d.ins_pos[d.nins++] = (uint8_t)b;
+    d.nops = (int)(i1 - i0);
+    int pos5[5], np = 0;
+    for (int b = 0; b < n; ++b)
+        if ((t5 >> b) & 1ULL) pos5[np++] = b;
+    for (int j = 0; j < 5; ++j) u.tslot[j] = (uint8_t)slot[pos5[j]];
+    uint32_t moff = 0;
+    for (size_t o = i0; o < i1; ++o) {
+        const GateOp& op = ops[o];
+        OpDesc& od = d.ops[o - i0];
+        od.ctrl_outer = op.ctrl_mask & ~tile;
+        uint32_t cl = 0;
+        for (int b = 0; b < n; ++b)
+            if (((op.ctrl_mask & tile) >> b) & 1ULL) cl |= 1u << slot[b];
+        od.ctrl_local = cl;
+        if (o == tc) {
+            od.k = 5;
+            od.tc = 1;
+            for (int j = 0; j < 5; ++j) od.tslot[j] = u.tslot[j];
+            continue;
+        }
+        od.k = op.k;
+        od.diag = op.diag ? 1 : 0;
+        for (int t = 0; t < op.k; ++t)
+            od.tslot[t] = ((tile >> op.pos[t]) & 1ULL) ? (uint8_t)slot[op.pos[t]] : (uint8_t)(kOuterSlot | op.pos[t]);
+        od.mat_off = moff;
+        moff += (uint32_t)op.m.size();
+    }
+    u.tc_op = (int)(tc - i0);
+    u.ew_bytes = (uint32_t)ewb;
+    u.gate_off = (uint32_t)((ewb + 1023) & ~(size_t)1023);
+
+    // TMA plan: the state as doubles, dimensions spanning consecutive
+    // positions: runs of tile positions (inside the box), gaps between them
+    // (coordinate from the tile base); when more than five dimensions would
+    // be needed, the last one spans everything above and the tile positions
+    // in it are fetched as separate copies.
+    struct Range {
+        int pos, bits;
+        bool tile;
+    };
+    std::vector<Range> ranges;
+    for (int b = 0; b < n;) {
+        const bool t = ((tile >> b) & 1ULL) != 0;
+        int e = b;
+        while (e < n && (((tile >> e) & 1ULL) != 0) == t) ++e;
+        int start = b;
+        // a box dimension spans at most 256 elements: 7 positions for the
+        // first (with the re/im pair), 8 for the others
+        while (start < e) {
+            const int cap = t ? (start == 0 ? 7 : 8) : 64;
+            const int len = std::min(cap, e - start);
+            ranges.push_back({start, len, t});
+            start += len;
+        }
+        b = e;
+    }
+    int rank = 0, tbits = 0;
+    for (size_t r = 0; r < ranges.size(); ++r) {
+        const bool last = r + 1 == ranges.size();
+        if (rank < 4 || last) {
+            u.dim_kind[rank] = ranges[r].tile ? 0 : 1;
+            u.dim_pos[rank] = (int8_t)ranges[r].pos;
+            u.dim_bits[rank] = (int8_t)ranges[r].bits;
+            if (ranges[r].tile) tbits += ranges[r].bits;
+            ++rank;
+            continue;
+        }
+        // rest: everything from this range up
+        u.dim_kind[rank] = 2;
+        u.dim_pos[rank] = (int8_t)ranges[r].pos;
+        u.dim_bits[rank] = (int8_t)(n - ranges[r].pos);
+        ++rank;
+        int ne = 0;
+        for (int b = ranges[r].pos; b < n; ++b)
+            if ((tile >> b) & 1ULL) u.extra_pos[ne++] = (int8_t)b;
+        u.nextra = (uint8_t)ne;
+        break;
+    }
+    u.rank = (uint8_t)rank;
+    if (tbits + u.nextra != kUmmaTileBits) return false;
+    u.box_bytes = 16u << tbits;
+    bytes = 2ULL * (1ULL << (n - popc64(fixed))) * 16;
+    return true;
+}
+
+void write_umma_pool(const UmmaDesc& u, const GateOp* ops, unsigned char* dst) {
+    const PassDesc& d = u.d;
+    for (int o = 0; o < d.nops; ++o) {
+        if (o == u.tc_op) continue;
+        // element-wise matrices in double-float (the tensor-core arithmetic's
+        // matrix format), untransposed
+        const GateOp& op = ops[o];
+        float* p = reinterpret_cast<float*>(dst + (size_t)d.ops[o].mat_off * 16);
+        for (size_t e = 0; e < op.m.size(); ++e) {
+            const double re = op.m[e].real(), im = op.m[e].imag();
+            const float hr = (float)re, hi = (float)im;
+            p[4 * e] = hr;
+            p[4 * e + 1] = hi;
+            p[4 * e + 2] = (float)(re - (double)hr);
+            p[4 * e + 3] = (float)(im - (double)hi);
+        }
+    }
+    int pos5[5];
+    for (int j = 0; j < 5; ++j) pos5[j] = d.tile_pos[u.tslot[j]];
+    build_umma_gate(ops[u.tc_op], pos5, dst + u.gate_off);
+}
+
+std::vector<LaunchPlan> plan_launches(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits, int max_ops,
+                                      bool allow_umma) {
+    std::vector<LaunchPlan> out;
+    const size_t nops = ops.size();
+    auto classic = [&](size_t a, size_t b) {
+        if (a >= b) return;
+        std::vector<size_t> first;
+        std::vector<PassPlan> pl = plan_passes(n, arith, ops.data() + a, b - a, max_tile_bits, max_ops, &first);
+        for (size_t i = 0; i < pl.size(); ++i) {
+            LaunchPlan L;
+            L.pass = pl[i];
+            L.first = a + first[i];
+            L.pool_bytes = pass_pool_bytes(arith, pl[i].desc);
+            L.bytes = pl[i].bytes;
+            out.push_back(L);
+        }
+    };
+    const bool umma = allow_umma && arith == kArithTC && n >= kUmmaTileBits;
+    size_t i = 0;
+    while (i < nops) {
+        size_t j = i;
+        if (umma)
+            while (j < nops && !umma_candidate(arith, ops[j])) ++j;
+        else
+            j = nops;
+        if (j == nops) {
+            classic(i, nops);
+            break;
+        }
+        // element-wise gates just before the dense gate join its pass
+        size_t p = j;
+        size_t ewb = 0;
+        while (p > i && elementwise_op(ops[p - 1]) && ewb + ew_pool_bytes(ops[p - 1]) <= kUmmaEwMaxBytes &&
+               j - p + 1 < (size_t)kMaxOpsPerPass) {
+            ewb += ew_pool_bytes(ops[p - 1]);
+            --p;
+        }
+        size_t e = j + 1;
+        while (e < nops && elementwise_op(ops[e]) && ewb + ew_pool_bytes(ops[e]) <= kUmmaEwMaxBytes &&
+               e - p < (size_t)kMaxOpsPerPass) {
+            ewb += ew_pool_bytes(ops[e]);
+            ++e;
+        }
+        LaunchPlan L;
+        uint64_t by = 0;
+        if (!build_umma(n, ops.data(), p, j, e, L.udesc, by)) {
+            classic(i, j + 1);
+            i = j + 1;
+            continue;
+        }
+        classic(i, p);
+        L.umma = true;
+        L.first = p;
+        L.pool_bytes = L.udesc.gate_off + kUmmaGateBytes;
+        L.bytes = by;
+        out.push_back(L);
+        i = e;
+    }
+    return out;
+}
+
 uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits,
                               int max_ops, uint64_t* passes_out) {
     if (ops.empty()) return 0;
+    if (arith == kArithTC && umma_enabled() && n >= kUmmaTileBits) {
+        std::vector<LaunchPlan> L = plan_launches(n, arith, ops, max_tile_bits, max_ops, true);
+        size_t total = 0;
+        for (auto& l : L) {
+            total = (total + 1023) & ~(size_t)1023;
+            l.pool_off = total;
+            total += (l.pool_bytes + 255) & ~(size_t)255;
+        }
+        total = std::max<size_t>(total, 256);
+        ensure_pinned(total);
+        ensure_pool(total);
+        unsigned char* host = static_cast<unsigned char*>(pinned_);
+        for (const auto& l : L) {
+            if (l.umma) write_umma_pool(l.udesc, ops.data() + l.first, host + l.pool_off);
+            else write_pass_pool(arith, l.pass.desc, ops.data() + l.first, host + l.pool_off);
+        }
+        cuda_check(cudaMemcpyAsync(pool_, pinned_, total, cudaMemcpyHostToDevice, stream_), "cudaMemcpyAsync(matrices)");
+        cuda_check(cudaEventRecord(staging_free_, stream_), "cudaEventRecord");
+        staging_pending_ = true;
+        uint64_t bytes = 0;
+        for (const auto& l : L) {
+            TimedLaunch tl{nullptr, nullptr, l.bytes};
+            if (timing_) {
+                tl.a = take_event();
+                tl.b = take_event();
+                cuda_check(cudaEventRecord(tl.a, stream_), "cudaEventRecord");
+            }
+            unsigned char* mats = static_cast<unsigned char*>(pool_) + l.pool_off;
+            if (l.umma) cuda_check(launch_umma_pass(state, mats, l.udesc, stream_), "launch_umma_pass");
+            else cuda_check(launch_pass(arith, state, mats, l.pass.desc, stream_), "launch_pass");
+            if (timing_) {
+                cuda_check(cudaEventRecord(tl.b, stream_), "cudaEventRecord");
+                timed_.push_back(tl);
+            }
+            bytes += l.bytes;
+        }
+        if (passes_out) *passes_out = L.size();
+        return bytes;
+    }
     std::vector<size_t> first;
     std::vector<PassPlan> plans = plan_passes(n, arith, ops, max_tile_bits, max_ops, &first);
     size_t total = 0;

@@ -51,6 +51,9 @@ public:
     Workspace& operator=(const Workspace&) = delete;
 
     cudaStream_t stream() const { return stream_; }
+    // Wait for the stream, then fail (CudaError) if a tensor-memory pass on
+    // this device ran out of one of its bounded waits since the last check.
+    void synchronize_checked();
     ReduceScratch& reduce() { return rs_; }
     // Device scratch of at least `bytes` (grown on demand; contents undefined).
     void* scratch(size_t bytes);
@@ -100,6 +103,30 @@ private:
     std::vector<cudaEvent_t> event_pool_;
     cudaEvent_t take_event();
 };
+
+// One launch of apply_ops: a tiled pass of the pass kernel, or a
+// tensor-memory pass (one dense gate on the tcgen05 tensor cores with the
+// diagonal / scalar gates around it, complex128 tensor-core arithmetic).
+struct LaunchPlan {
+    bool umma = false;
+    PassPlan pass;          // tiled pass (pass.pool_off unused)
+    UmmaDesc udesc;         // tensor-memory pass
+    size_t first = 0;       // index of the launch's first op
+    size_t pool_off = 0;    // byte offset of the launch's matrices in the pool
+    size_t pool_bytes = 0;
+    uint64_t bytes = 0;     // algorithmic HBM bytes of the sweep
+};
+// Whether apply_ops may use tensor-memory passes (HQS_UMMA=0 turns them off).
+bool umma_enabled();
+// Whether a gate can be the dense gate of a tensor-memory pass.
+bool umma_candidate(int arith, const GateOp& op);
+// The launches apply_ops makes for ops: tensor-memory passes around every
+// candidate dense gate (when allowed and n >= 12), the pass planner for the
+// rest.
+std::vector<LaunchPlan> plan_launches(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits, int max_ops,
+                                      bool allow_umma);
+// Matrices of a tensor-memory pass (ops: the pass's gates, in order).
+void write_umma_pool(const UmmaDesc& u, const GateOp* ops, unsigned char* dst);
 
 // Bytes of a planned pass's matrix pool and the pool itself (ops are the
 // pass's gates, in order), in the arithmetic's element format.

@@ -275,6 +275,28 @@ typedef struct {
 int hqs_plan_passes(int n, int arith, int nops, const int* k, const int* pos, const uint64_t* ctrl, const int* diag,
                     int max_tile_bits, int max_ops, hqs_pass_info* out, size_t cap, size_t* npasses);
 
+/* The launches hqs_apply_gates makes for the same gates, computed on the host
+ * (no GPU): with HQS_ARITH_TC on states of 12 or more qubits, every dense
+ * gate on 3-5 qubits gets a tensor-memory pass (tcgen05 tensor cores, TMA tile
+ * copies) together with the diagonal / scalar gates around it; the rest are
+ * tiled passes as in hqs_plan_passes. No reference counterpart (the reference
+ * runs one sweep per fused gate, SimulatorMPI.cpp:441-541). *nlaunches
+ * receives the count; the first cap launches are described in out. */
+typedef struct {
+    uint32_t first_op, nops;   /* the launch applies gates [first_op, first_op + nops) */
+    uint32_t umma;             /* 1: tensor-memory pass */
+    uint32_t tc_op;            /* tensor-memory pass: index (within the launch) of the dense gate */
+    uint64_t tile_mask;        /* state positions in the tile */
+    uint64_t target_mask;      /* tensor-memory pass: the five target positions (padded) */
+    uint64_t fixed_mask;       /* control positions outside the tile every gate shares */
+    uint32_t rank, nextra;     /* tensor-memory pass: TMA tensor rank, tile bits fetched as separate copies */
+    uint32_t box_bytes;        /* tensor-memory pass: bytes of one TMA box */
+    int32_t dim_kind[5], dim_pos[5], dim_bits[5];  /* TMA dimensions: 0 box, 1 gap, 2 rest; first position; positions */
+    uint64_t pool_bytes, sweep_bytes;
+} hqs_launch_info;
+int hqs_plan_launches(int n, int arith, int nops, const int* k, const int* pos, const uint64_t* ctrl, const int* diag,
+                      int max_tile_bits, int max_ops, hqs_launch_info* out, size_t cap, size_t* nlaunches);
+
 int hqs_apply_gates(hqs_ws* ws, void* state, int n, int arith, int nops, const int* k, const int* pos,
                     const uint64_t* ctrl, const int* diag, const double* mats, int max_tile_bits, int max_ops,
                     uint64_t* bytes_out, uint64_t* passes_out);

@@ -113,3 +113,79 @@ def test_invalid_gates_rejected(hqs):
         capi.plan_passes(10, "tc", [(1, [2], 1 << 2, False)])
     with pytest.raises(capi.HQSError):
         capi.plan_passes(10, "auto", [(1, [2], 0, False)])
+
+
+# ------------------------------------------------------- tensor-memory passes
+
+def _check_umma_launch(n, L, gates):
+    tile = L["tile_mask"]
+    assert bin(tile).count("1") == 12
+    tmask = L["target_mask"]
+    assert bin(tmask).count("1") == 5 and tmask & tile == tmask
+    g = gates[L["first_op"] + L["tc_op"]]
+    for p in g[1]:
+        assert (tmask >> p) & 1
+    assert tmask & g[2] == 0  # controls are never targets of the widened gate
+    # TMA dimensions cover positions 0..n-1 in order; box dimensions are runs
+    # of tile positions (at most 256 elements), gaps hold no tile position,
+    # the rest dimension (if any) is last and its tile positions are copies
+    pos, tbits = 0, 0
+    rank = L["rank"]
+    assert 1 <= rank <= 5
+    for i in range(rank):
+        kind, p, b = L["dim_kind"][i], L["dim_pos"][i], L["dim_bits"][i]
+        assert p == pos and b >= 1
+        span = ((1 << b) - 1) << p
+        if kind == 0:
+            assert span & tile == span
+            assert b <= (7 if i == 0 else 8)
+            tbits += b
+        elif kind == 1:
+            assert span & tile == 0
+        else:
+            assert kind == 2 and i == rank - 1
+            assert bin(span & tile).count("1") == L["nextra"]
+        pos += b
+    assert pos == n
+    assert tbits + L["nextra"] == 12
+    assert L["box_bytes"] == 16 << tbits
+
+
+def test_umma_launch_plans_cover_gates_and_tile():
+    rng = np.random.default_rng(21)
+    for trial in range(60):
+        n = int(rng.integers(12, 35))
+        gates = []
+        for _ in range(int(rng.integers(1, 12))):
+            kind = rng.integers(0, 4)
+            k = int(rng.integers(1, 6))
+            pos = [int(x) for x in rng.choice(n, size=k, replace=False)]
+            ctrl = 0
+            if rng.random() < 0.2:
+                free = [b for b in range(n) if b not in pos]
+                ctrl = 1 << int(rng.choice(free))
+            gates.append((k, pos, ctrl, kind == 0))
+        launches = capi.plan_launches(n, "tc", gates)
+        nxt = 0
+        for L in launches:
+            assert L["first_op"] == nxt
+            nxt += L["nops"]
+            if L["umma"]:
+                _check_umma_launch(n, L, gates)
+                ops = gates[L["first_op"]:L["first_op"] + L["nops"]]
+                dense = [i for i, g in enumerate(ops) if not g[3] and g[0] >= 3]
+                assert dense == [L["tc_op"]]
+                assert all(g[3] or g[0] == 0 or i == L["tc_op"] for i, g in enumerate(ops))
+        assert nxt == len(gates)
+        # every dense 3-5 qubit gate runs in a tensor-memory pass
+        umma_gates = {L["first_op"] + L["tc_op"] for L in launches if L["umma"]}
+        for i, g in enumerate(gates):
+            if not g[3] and g[0] >= 3:
+                assert i in umma_gates
+
+
+def test_umma_not_used_below_twelve_qubits_or_other_arithmetic():
+    gates = [(5, [0, 2, 4, 6, 8], 0, False)]
+    assert not any(L["umma"] for L in capi.plan_launches(11, "tc", gates))
+    assert not any(L["umma"] for L in capi.plan_launches(20, "df", gates))
+    assert any(L["umma"] for L in capi.plan_launches(20, "tc", gates))
