@@ -31,18 +31,38 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* m, uint32_t byte
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(m)), "r"(bytes) : "memory");
 }
 
-// Wait for the phase with the given parity to complete. Bounded: after
-// kWaitLimit polls (each poll itself blocks for a hardware-defined slice),
-// or as soon as another thread of the CTA has raised *abort, it returns
-// false; the caller then records the failure and leaves its loop.
-constexpr uint32_t kWaitLimit = 1u << 22;
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Wait for the phase with the given parity to complete. Bounded in time:
+// after kWaitNs nanoseconds (far above any legitimate wait of the pass, which
+// is one tile's copy or compute time, microseconds) it raises *abort and
+// returns false; it also returns false as soon as another thread of the CTA
+// has raised *abort. The caller then leaves its loop.
+constexpr uint64_t kWaitNs = 2000000000ULL;
 __device__ __forceinline__ bool mbar_wait(uint64_t* m, uint32_t parity, volatile int* abort) {
-    for (uint32_t i = 0; i < kWaitLimit; ++i) {
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t i = 0;; ++i) {
         if (mbar_try(m, parity)) return true;
-        if ((i & 255u) == 255u && *abort) return false;
+        if ((i & 63u) == 63u) {
+            if (*abort) return false;
+            if (globaltimer_ns() - t0 > kWaitNs) {
+                *abort = 1;
+                return false;
+            }
+        }
     }
-    *abort = 1;
-    return false;
+}
+// The same wait without the abort flag (tear-down: copies or MMAs in flight).
+__device__ __forceinline__ bool mbar_wait_quiet(uint64_t* m, uint32_t parity) {
+    const uint64_t t0 = globaltimer_ns();
+    for (uint32_t i = 0;; ++i) {
+        if (mbar_try(m, parity)) return true;
+        if ((i & 63u) == 63u && globaltimer_ns() - t0 > kWaitNs) return false;
+    }
 }
 
 // ------------------------------------------------------------------ fences

@@ -358,9 +358,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             // loads still in flight (a loop left early): wait for them before
             // the CTA's shared memory goes away
             for (int s = 0; s < 2; ++s)
-                if (issued[s])
-                    for (uint32_t i = 0; i < kWaitLimit && !mbar_try(&full[s], (issued[s] - 1) & 1u); ++i) {
-                    }
+                if (issued[s]) mbar_wait_quiet(&full[s], (issued[s] - 1) & 1u);
         }
         __syncwarp();
     } else if (warp == kMmaWarp) {
@@ -401,8 +399,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
         }
         if (committed > 0 && lane == 0) {
             // the last MMAs must be complete before tensor memory is freed
-            for (uint32_t i = 0; i < kWaitLimit && !mbar_try(mbar, (uint32_t)((committed - 1) & 1)); ++i) {
-            }
+            mbar_wait_quiet(mbar, (uint32_t)((committed - 1) & 1));
         }
         __syncwarp();
     } else {
@@ -473,8 +470,11 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             bar_sync(1, kCompute);
             if (*abort) break;
             fence_after_sync();
-            if (act && (gb[g] & tc.ctrl_local) == tc.ctrl_local) {
-                // outputs: group g, output reals 32 half .. 32 half + 31
+            if (act) {
+                // outputs: group g, output reals 32 half .. 32 half + 31. The
+                // tensor-memory loads are warp-collective: every thread takes
+                // part; a group whose controls are not all 1 keeps its inputs.
+                const bool write = (gb[g] & tc.ctrl_local) == tc.ctrl_local;
                 const int Eb = erow[g];
                 const uint32_t gbase = gb[g];
 #pragma unroll
@@ -495,7 +495,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
                                                 __uint_as_float(r[4][c]), __uint_as_float(r[5][c])};
                             out[p] = Eb == 0 ? 0.0 : level_sum_to_double(S, Eb + ecol[n0 + c] - 2059);
                         }
-                        buf[gbase | offt[(n0 >> 1) + a]] = make_double2(out[0], out[1]);
+                        if (write) buf[gbase | offt[(n0 >> 1) + a]] = make_double2(out[0], out[1]);
                     }
                 }
             }
