@@ -82,7 +82,8 @@ constexpr int kUmmaGroups = 128;
 constexpr int kUmmaDigits = 6;
 constexpr uint32_t kUmmaGatePlaneBytes = 6 * 64 * 128;           // six gate digit planes, 64 rows x 128 B
 constexpr uint32_t kUmmaGateBytes = kUmmaGatePlaneBytes + 64 * 4;  // + column exponents
-constexpr uint32_t kUmmaEwMaxBytes = 12 * 1024;                    // element-wise matrices staged per pass
+constexpr uint32_t kUmmaEwMaxBytes = 7 * 1024;                     // element-wise matrices staged per pass
+constexpr int kUmmaRunBits = 8;                                    // tile bits a diagonal run's factor may depend on
 
 struct UmmaDesc {
     PassDesc d;            // tile (q = 12), fixed mask, ops; ops[tc_op] is the dense gate
@@ -99,6 +100,8 @@ struct UmmaDesc {
     int8_t dim_pos[5];     // first state position of each dimension
     int8_t dim_bits[5];    // state positions each dimension spans
     int8_t extra_pos[kMaxTileBits];  // state positions of the extra tile bits, ascending
+    uint32_t run_mask[2];  // tile slots the element-wise run before (0) / after (1) the dense gate
+                           // depends on (targets and controls inside the tile), at most kUmmaRunBits
 };
 
 // true when any op of the pass runs on the tensor cores

@@ -65,7 +65,9 @@ constexpr uint32_t kSmGb = kSmMx + 1024;    // uint16[128]: tile index of each g
 constexpr uint32_t kSmOff = kSmGb + 256;    // uint16[32]: tile offset of each input
 constexpr uint32_t kSmBar = kSmOff + 64;    // 6 mbarriers
 constexpr uint32_t kSmMisc = kSmBar + 64;   // tensor-memory base, abort flag
-constexpr uint32_t kSmEw = kSmMisc + 64;    // element-wise matrices (float4)
+constexpr uint32_t kSmLut = kSmMisc + 64;   // uint8[2][2][64]: factor-table index of tile slots 0-5 / 6-11
+constexpr uint32_t kSmTab = kSmLut + 256;   // float4[2][256]: the runs' factor tables of the current tile
+constexpr uint32_t kSmEw = kSmTab + 2 * (1u << kUmmaRunBits) * 16;  // element-wise matrices (float4)
 constexpr uint32_t kSmBytes = kSmEw + kUmmaEwMaxBytes + 1024;  // + alignment slack
 
 // tensor-memory columns: six level regions of 64, then state planes 0-3
@@ -210,29 +212,49 @@ __device__ __forceinline__ double level_sum_to_double(const float (&S)[6], int o
 }
 
 // ------------------------------------------------------------------ element-wise runs
-// ops [o0, o1) of the pass (diagonal / scalar), in place on the tile, by the
-// compute threads
-__device__ __forceinline__ void ew_run(double2* buf, const float4* __restrict__ pool, const PassDesc& d, int o0,
-                                       int o1, uint64_t base) {
-    for (int L = threadIdx.x; L < 4096; L += kCompute) {
-        float4 x = ArithDFRaw::elem_load(buf[L]);
-        for (int o = o0; o < o1; ++o) {
-            const OpDesc& op = d.ops[o];
-            if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
-            if (op.k == 0) {
-                x = ArithDFRaw::elem_mul(pool[op.mat_off], x);
-                continue;
-            }
-            if (((uint32_t)L & op.ctrl_local) != op.ctrl_local) continue;
-            int r = 0;
-            for (int j = 0; j < op.k; ++j) {
-                const int sl = op.tslot[j];
-                const uint64_t bit = (sl & kOuterSlot) ? (base >> (sl & 63)) : ((uint64_t)L >> sl);
-                r |= (int)(bit & 1ULL) << j;
-            }
-            x = ArithDFRaw::elem_mul(pool[op.mat_off + r], x);
+// A run of diagonal / scalar gates multiplies every amplitude by the product
+// of its gates' entries. Within one tile that product depends only on the
+// run's target and control slots inside the tile (at most kUmmaRunBits; the
+// positions outside the tile are fixed by the tile base), so each tile first
+// tabulates it (double-float, one entry per combination of those slots) and
+// every amplitude then takes one table entry.
+
+// pext of a 12-bit tile index over the run's slots, from two 64-entry tables
+__device__ __forceinline__ uint32_t run_index(const uint8_t* lut, uint32_t L) { return lut[L & 63u] | lut[64 + (L >> 6)]; }
+
+// table entry i: the run's product at the tile index whose run slots hold i
+__device__ __forceinline__ float4 run_entry(const float4* __restrict__ pool, const PassDesc& d, int o0, int o1,
+                                            uint32_t mask, uint32_t i, uint64_t base) {
+    uint32_t L = 0;
+    for (int sl = 0; sl < 12; ++sl)
+        if ((mask >> sl) & 1u) {
+            L |= (i & 1u) << sl;
+            i >>= 1;
         }
-        buf[L] = ArithDFRaw::elem_store(x);
+    float4 x = make_float4(1.f, 0.f, 0.f, 0.f);
+    for (int o = o0; o < o1; ++o) {
+        const OpDesc& op = d.ops[o];
+        if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
+        if (op.k == 0) {
+            x = ArithDF::mul(pool[op.mat_off], x);
+            continue;
+        }
+        if ((L & op.ctrl_local) != op.ctrl_local) continue;
+        int r = 0;
+        for (int j = 0; j < op.k; ++j) {
+            const int sl = op.tslot[j];
+            const uint64_t bit = (sl & kOuterSlot) ? (base >> (sl & 63)) : ((uint64_t)L >> sl);
+            r |= (int)(bit & 1ULL) << j;
+        }
+        x = ArithDF::mul(pool[op.mat_off + r], x);
+    }
+    return x;
+}
+
+__device__ __forceinline__ void run_apply(double2* buf, const float4* tab, const uint8_t* lut) {
+    for (int L = threadIdx.x; L < 4096; L += kCompute) {
+        const float4 x = ArithDFRaw::elem_load(buf[L]);
+        buf[L] = ArithDFRaw::elem_store(ArithDF::mul(tab[run_index(lut, (uint32_t)L)], x));
     }
 }
 
@@ -257,6 +279,8 @@ __global__ void __launch_bounds__(kThreadsU, 1)
     uint16_t* gb = reinterpret_cast<uint16_t*>(sm + kSmGb);
     uint16_t* offt = reinterpret_cast<uint16_t*>(sm + kSmOff);
     const float4* ewp = reinterpret_cast<const float4*>(sm + kSmEw);
+    uint8_t* lut = sm + kSmLut;
+    float4* tab = reinterpret_cast<float4*>(sm + kSmTab);
 
     const uint64_t ntiles = 1ULL << (d.n - d.nins);
     const uint64_t my_n = (uint64_t)blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
@@ -295,6 +319,18 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             uint32_t v = 0;
             for (int j = 0; j < 5; ++j) v |= ((e >> j) & 1u) << u.tslot[j];
             offt[e] = (uint16_t)v;
+        }
+        // factor-table index of tile slots 0-5 and 6-11, per run
+        for (int t = threadIdx.x; t < 256; t += kCompute) {
+            const int r = t >> 7, hi = (t >> 6) & 1;
+            const uint32_t v = (uint32_t)(t & 63) << (hi * 6), m = u.run_mask[r];
+            uint32_t idx = 0, k = 0;
+            for (int sl = 0; sl < 12; ++sl)
+                if ((m >> sl) & 1u) {
+                    idx |= ((v >> sl) & 1u) << k;
+                    ++k;
+                }
+            lut[t] = (uint8_t)idx;
         }
     }
     fence_proxy_async();
@@ -415,8 +451,19 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             mbar_wait(&full[s], (uint32_t)((it >> 1) & 1), abort);
             bar_sync(1, kCompute);
             if (*abort) break;
-            if (u.tc_op > 0) {
-                ew_run(buf, ewp, d, 0, u.tc_op, base);
+            const bool pre = u.tc_op > 0, post = u.tc_op + 1 < d.nops;
+            if (pre || post) {
+                for (int t = threadIdx.x; t < 2 * (1 << kUmmaRunBits); t += kCompute) {
+                    const int r = t >> kUmmaRunBits;
+                    const uint32_t i = (uint32_t)t & ((1u << kUmmaRunBits) - 1u);
+                    if ((r == 0 && !pre) || (r == 1 && !post) || i >= (1u << __popc(u.run_mask[r]))) continue;
+                    tab[t] = r == 0 ? run_entry(ewp, d, 0, u.tc_op, u.run_mask[0], i, base)
+                                    : run_entry(ewp, d, u.tc_op + 1, d.nops, u.run_mask[1], i, base);
+                }
+                bar_sync(1, kCompute);
+            }
+            if (pre) {
+                run_apply(buf, tab, lut);
                 bar_sync(1, kCompute);
             }
             const bool act = (base & tc.ctrl_outer) == tc.ctrl_outer;
@@ -501,8 +548,8 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             }
             fence_before_sync();
             bar_sync(1, kCompute);
-            if (u.tc_op + 1 < d.nops) {
-                ew_run(buf, ewp, d, u.tc_op + 1, d.nops, base);
+            if (post) {
+                run_apply(buf, tab + (1 << kUmmaRunBits), lut + 128);
                 bar_sync(1, kCompute);
             }
             fence_proxy_async();

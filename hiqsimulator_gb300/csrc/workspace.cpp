@@ -581,16 +581,19 @@ static void build_umma_gate(const GateOp& g, const int (&pos5)[5], unsigned char
 // Tensor-memory pass over ops [i0, i1) with the dense gate at tc. Tile: the
 // gate's targets, then the lowest other positions up to 12; when the gate has
 // fewer than five targets, the highest of those positions that are not its
-// controls become extra targets with identity factors. Returns false when the
-// pass cannot be formed (state too small, element-wise matrices too large).
-static bool build_umma(int n, const GateOp* ops, size_t i0, size_t tc, size_t i1, UmmaDesc& u, uint64_t& bytes) {
+// controls become extra targets with identity factors. Returns kUmmaOk, or
+// why the pass cannot be formed: the run before / after the dense gate
+// depends on too many tile slots, or another reason (state too small,
+// element-wise matrices too large).
+enum { kUmmaOk = 0, kUmmaPreWide = 1, kUmmaPostWide = 2, kUmmaNo = 3 };
+static int build_umma(int n, const GateOp* ops, size_t i0, size_t tc, size_t i1, UmmaDesc& u, uint64_t& bytes) {
     const GateOp& g = ops[tc];
     uint64_t tmask = 0;
     for (int t = 0; t < g.k; ++t) tmask |= 1ULL << g.pos[t];
     std::vector<int> picks;
     for (int b = 0; b < n && (int)picks.size() < kUmmaTileBits - g.k; ++b)
         if (!((tmask >> b) & 1ULL)) picks.push_back(b);
-    if ((int)picks.size() < kUmmaTileBits - g.k) return false;
+    if ((int)picks.size() < kUmmaTileBits - g.k) return kUmmaNo;
     uint64_t t5 = tmask;
     int extra_t = 5 - g.k;
     for (int i = (int)picks.size() - 1; i >= 0 && extra_t > 0; --i)
@@ -598,13 +601,13 @@ static bool build_umma(int n, const GateOp* ops, size_t i0, size_t tc, size_t i1
             t5 |= 1ULL << picks[i];
             --extra_t;
         }
-    if (extra_t > 0) return false;
+    if (extra_t > 0) return kUmmaNo;
     uint64_t tile = tmask;
     for (int p : picks) tile |= 1ULL << p;
     size_t ewb = 0;
     for (size_t o = i0; o < i1; ++o)
         if (o != tc) ewb += ew_pool_bytes(ops[o]);
-    if (ewb > kUmmaEwMaxBytes || i1 - i0 > (size_t)kMaxOpsPerPass) return false;
+    if (ewb > kUmmaEwMaxBytes || i1 - i0 > (size_t)kMaxOpsPerPass) return kUmmaNo;
 
     std::memset(&u, 0, sizeof(u));
     PassDesc& d = u.d;
@@ -648,11 +651,18 @@ static bool build_umma(int n, const GateOp* ops, size_t i0, size_t tc, size_t i1
         }
         od.k = op.k;
         od.diag = op.diag ? 1 : 0;
-        for (int t = 0; t < op.k; ++t)
-            od.tslot[t] = ((tile >> op.pos[t]) & 1ULL) ? (uint8_t)slot[op.pos[t]] : (uint8_t)(kOuterSlot | op.pos[t]);
+        uint32_t rm = cl;
+        for (int t = 0; t < op.k; ++t) {
+            const bool in = ((tile >> op.pos[t]) & 1ULL) != 0;
+            od.tslot[t] = in ? (uint8_t)slot[op.pos[t]] : (uint8_t)(kOuterSlot | op.pos[t]);
+            if (in) rm |= 1u << slot[op.pos[t]];
+        }
+        u.run_mask[o < tc ? 0 : 1] |= rm;
         od.mat_off = moff;
         moff += (uint32_t)op.m.size();
     }
+    if (__builtin_popcount(u.run_mask[0]) > kUmmaRunBits) return kUmmaPreWide;
+    if (__builtin_popcount(u.run_mask[1]) > kUmmaRunBits) return kUmmaPostWide;
     u.tc_op = (int)(tc - i0);
     u.ew_bytes = (uint32_t)ewb;
     u.gate_off = (uint32_t)((ewb + 1023) & ~(size_t)1023);
@@ -705,10 +715,10 @@ static bool build_umma(int n, const GateOp* ops, size_t i0, size_t tc, size_t i1
         break;
     }
     u.rank = (uint8_t)rank;
-    if (tbits + u.nextra != kUmmaTileBits) return false;
+    if (tbits + u.nextra != kUmmaTileBits) return kUmmaNo;
     u.box_bytes = 16u << tbits;
     bytes = 2ULL * (1ULL << (n - popc64(fixed))) * 16;
-    return true;
+    return kUmmaOk;
 }
 
 void write_umma_pool(const UmmaDesc& u, const GateOp* ops, unsigned char* dst) {
@@ -778,7 +788,15 @@ std::vector<LaunchPlan> plan_launches(int n, int arith, const std::vector<GateOp
         }
         LaunchPlan L;
         uint64_t by = 0;
-        if (!build_umma(n, ops.data(), p, j, e, L.udesc, by)) {
+        int st;
+        // leave out gates of the runs until each run's factor depends on at
+        // most kUmmaRunBits tile slots
+        while ((st = build_umma(n, ops.data(), p, j, e, L.udesc, by)) == kUmmaPreWide ||
+               st == kUmmaPostWide) {
+            if (st == kUmmaPreWide) ++p;
+            else --e;
+        }
+        if (st != kUmmaOk) {
             classic(i, j + 1);
             i = j + 1;
             continue;
