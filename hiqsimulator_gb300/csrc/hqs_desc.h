@@ -82,7 +82,7 @@ constexpr int kUmmaGroups = 128;
 constexpr int kUmmaDigits = 6;
 constexpr uint32_t kUmmaGatePlaneBytes = 6 * 64 * 128;           // six gate digit planes, 64 rows x 128 B
 constexpr uint32_t kUmmaGateBytes = kUmmaGatePlaneBytes + 64 * 4;  // + column exponents
-constexpr uint32_t kUmmaEwMaxBytes = 7 * 1024;                     // element-wise matrices staged per pass
+constexpr uint32_t kUmmaEwMaxBytes = 13 * 512;                     // element-wise matrices staged per pass
 constexpr int kUmmaRunBits = 8;                                    // tile bits a diagonal run's factor may depend on
 
 struct UmmaDesc {

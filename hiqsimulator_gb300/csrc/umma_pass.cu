@@ -24,9 +24,10 @@
 // side along N, accumulates each (i, j) product directly into the region of
 // level i + j: one MMA covers up to four levels (N = 256).
 //
-// Warps: 0-7 split digits and assemble outputs (CUDA cores), warp 8 moves
-// tiles with TMA tensor copies (load into one of two tile buffers, store back
-// from it), warp 9 allocates tensor memory and issues the MMAs. Every wait is
+// Warps: 0-15 split digits and assemble outputs (CUDA cores; four per warp
+// scheduler), warp 16 moves tiles with TMA tensor copies (load into one of
+// two tile buffers, store back from it), warp 17 allocates tensor memory and
+// issues the MMAs. Every wait is
 // bounded; a wait that runs out raises a CTA-wide abort flag, every warp
 // leaves its loop, the TMA warp waits (bounded) for its copies in flight, the
 // MMA warp for its MMAs, tensor memory is freed and the host sees the error
@@ -49,9 +50,9 @@ namespace {
 
 using namespace tc05;
 
-constexpr int kCompute = 256;  // warps 0..7
-constexpr int kTmaWarp = 8, kMmaWarp = 9;
-constexpr int kThreadsU = 320;
+constexpr int kCompute = 512;  // warps 0..15
+constexpr int kTmaWarp = 16, kMmaWarp = 17;
+constexpr int kThreadsU = 576;
 
 // shared memory, relative to a 1024-byte aligned base
 constexpr uint32_t kSmGate = 0;             // 6 gate digit planes, 64 rows x 128 B each
@@ -60,8 +61,8 @@ constexpr uint32_t kSmTile0 = 81920;        // tile buffers, 4096 x double2
 constexpr uint32_t kSmTile1 = 147456;
 constexpr uint32_t kSmEcol = 212992;        // int[64]: gate column exponents
 constexpr uint32_t kSmErow = kSmEcol + 256; // int[128]: group exponents of the current tile
-constexpr uint32_t kSmMx = kSmErow + 512;   // uint32[256]: half-group maxima
-constexpr uint32_t kSmGb = kSmMx + 1024;    // uint16[128]: tile index of each group's input 0
+constexpr uint32_t kSmMx = kSmErow + 512;   // uint32[512]: quarter-group maxima
+constexpr uint32_t kSmGb = kSmMx + 2048;    // uint16[128]: tile index of each group's input 0
 constexpr uint32_t kSmOff = kSmGb + 256;    // uint16[32]: tile offset of each input
 constexpr uint32_t kSmBar = kSmOff + 64;    // 6 mbarriers
 constexpr uint32_t kSmMisc = kSmBar + 64;   // tensor-memory base, abort flag
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
         __syncwarp();
     } else {
         // ---- compute warps: digits, then outputs
-        const int q4 = warp & 3, half = warp >> 2, g = q4 * 32 + lane;
+        const int q4 = warp & 3, part = warp >> 2, g = q4 * 32 + lane;
         const OpDesc& tc = d.ops[u.tc_op];
         const uint32_t lane_base = (uint32_t)(q4 * 32) << 16;
         const Walk walk(d, blockIdx.x, gridDim.x);
@@ -469,42 +470,41 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             const bool act = (base & tc.ctrl_outer) == tc.ctrl_outer;
             if (act) {
                 // digit planes of the tile's 128 groups; this thread: group g,
-                // inputs 16 half .. 16 half + 15
+                // inputs 8 part .. 8 part + 7
                 const uint32_t gbase = gb[g];
-                double2 x[16];
+                double2 x[8];
                 uint32_t mx = 0;
 #pragma unroll
-                for (int i = 0; i < 16; ++i) {
-                    x[i] = buf[gbase | offt[half * 16 + i]];
+                for (int i = 0; i < 8; ++i) {
+                    x[i] = buf[gbase | offt[part * 8 + i]];
                     mx = max(mx, (uint32_t)__double2hiint(x[i].x) & 0x7FFFFFFFu);
                     mx = max(mx, (uint32_t)__double2hiint(x[i].y) & 0x7FFFFFFFu);
                 }
                 mxs[threadIdx.x] = mx;
                 bar_sync(1, kCompute);
-                const int Eb = (int)(max(mxs[g], mxs[128 + g]) >> 20);
-                if (half == 0) erow[g] = Eb;
+                const int Eb = (int)(max(max(mxs[g], mxs[128 + g]), max(mxs[256 + g], mxs[384 + g])) >> 20);
+                if (part == 0) erow[g] = Eb;
 #pragma unroll
                 for (int bt = 0; bt < 2; ++bt) {
-                    uint32_t pl[6][8];
+                    uint32_t pl[6][4];
 #pragma unroll
-                    for (int i = 0; i < 8; ++i) {
+                    for (int i = 0; i < 4; ++i) {
                         float dr[6], di[6];
-                        digits6(x[bt * 8 + i].x, Eb, dr);
-                        digits6(x[bt * 8 + i].y, Eb, di);
+                        digits6(x[bt * 4 + i].x, Eb, dr);
+                        digits6(x[bt * 4 + i].y, Eb, di);
 #pragma unroll
                         for (int p = 0; p < 6; ++p) pl[p][i] = pack_h2(dr[p], di[p]);
                     }
-                    const uint32_t e0 = (uint32_t)(half * 16 + bt * 8);
+                    const uint32_t e0 = (uint32_t)(part * 8 + bt * 4);
 #pragma unroll
-                    for (int p = 0; p < 4; ++p) tmem_st8(tmem + lane_base + kTmPlanes + (uint32_t)p * 32u + e0, pl[p]);
+                    for (int p = 0; p < 4; ++p)
+                        tmem_st4(tmem + lane_base + kTmPlanes + (uint32_t)p * 32u + e0, pl[p][0], pl[p][1], pl[p][2], pl[p][3]);
                     const uint32_t c0 = e0 >> 2;
 #pragma unroll
                     for (int p = 4; p < 6; ++p) {
                         unsigned char* row = sm + kSmPlanes + (uint32_t)(p - 4) * 16384u + (uint32_t)g * 128u;
                         *reinterpret_cast<uint4*>(row + ((c0 ^ (g & 7)) << 4)) =
                             make_uint4(pl[p][0], pl[p][1], pl[p][2], pl[p][3]);
-                        *reinterpret_cast<uint4*>(row + (((c0 + 1) ^ (g & 7)) << 4)) =
-                            make_uint4(pl[p][4], pl[p][5], pl[p][6], pl[p][7]);
                     }
                 }
                 tmem_st_wait();
@@ -518,15 +518,15 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             if (*abort) break;
             fence_after_sync();
             if (act) {
-                // outputs: group g, output reals 32 half .. 32 half + 31. The
+                // outputs: group g, output reals 16 part .. 16 part + 15. The
                 // tensor-memory loads are warp-collective: every thread takes
                 // part; a group whose controls are not all 1 keeps its inputs.
                 const bool write = (gb[g] & tc.ctrl_local) == tc.ctrl_local;
                 const int Eb = erow[g];
                 const uint32_t gbase = gb[g];
 #pragma unroll
-                for (int ch = 0; ch < 4; ++ch) {
-                    const uint32_t n0 = (uint32_t)(half * 32 + ch * 8);
+                for (int ch = 0; ch < 2; ++ch) {
+                    const uint32_t n0 = (uint32_t)(part * 16 + ch * 8);
                     uint32_t r[6][8];
 #pragma unroll
                     for (int lev = 0; lev < 6; ++lev) tmem_ld8(tmem + lane_base + (uint32_t)lev * 64u + n0, r[lev]);
