@@ -185,13 +185,16 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per pass-kernel launch from the committed ncu summary
-    (profiles/pass_kernel_traffic.json), scaled to the state's amplitudes."""
-    p = os.path.join(ROOT, "profiles", "pass_kernel_traffic.json")
+def profile_traffic(kernel):
+    """DRAM bytes per launch of a kernel from the committed ncu summaries
+    (profiles/kernel_traffic.json: bytes per amplitude of one launch,
+    measured on a smaller state), scaled to the state's amplitudes."""
+    p = os.path.join(ROOT, "profiles", "kernel_traffic.json")
     if not os.path.exists(p):
         return None
-    d = json.load(open(p))
+    d = json.load(open(p)).get(kernel)
+    if not d:
+        return None
     return float(d["bytes_per_amplitude"]) * (1 << N_QUBITS)
 
 
@@ -387,16 +390,19 @@ def serving_report(args):
 def precision_report(qubits=28, layers=40, cluster=5):
     """Precision workload: a brickwork of Haar U(4) on alternating pairs,
     greedy-fused into blocks of up to `cluster` qubits, run as complex128
-    (tensor-core digit mode, the parity-tested reference at this size) and as
-    complex64 in FP32, in two-digit tensor-core mode and in 3xTF32; each
-    complex64 state against the complex128 one (fidelity, normalized
-    fidelity, norm, max error) and the device time of each (second replay)."""
+    (tensor-core digit mode) and as complex64 in FP32, in two-digit
+    tensor-core mode and in 3xTF32. Every state is compared with the
+    oracle's FP64 state of the same circuit (the checker: oracle/, on the
+    host cores): fidelity, normalized fidelity, norm and max amplitude
+    error; device time of each mode (second replay) against complex128."""
     import hiqsimulator_gb300 as hqs
     from hiqsimulator_gb300 import circuits
+    from oracle.engine import OracleSimulator
     qs = list(range(qubits))
     gates = circuits.brickwork(2024, qs, layers)
     cmds = circuits.greedy_stream(gates, qs, cluster)
-    out = {"workload": "%dq brickwork, %d layers of Haar U(4), greedy fusion k<=%d" % (qubits, layers, cluster)}
+    out = {"workload": "%dq brickwork, %d layers of Haar U(4), greedy fusion k<=%d" % (qubits, layers, cluster),
+           "against": "oracle FP64 state of the same fused circuit"}
     states = {}
     modes = (("c128_tc", "c128", "tc"), ("c64_f32", "c64", "f32"), ("c64_tc", "c64", "tc"), ("c64_tf32", "c64", "tf32"))
     for key, prec, arith in modes:
@@ -410,20 +416,234 @@ def precision_report(qubits=28, layers=40, cluster=5):
             circuits.replay(sim, cmds)
             times.append(sim.timer_stop())
             if rep == 0:
-                _, states[key] = sim.cheat_local_numpy()
+                m, v = sim.cheat_local_numpy()
+                ident = {q: q for q in qs}
+                if dict(m) != ident:  # bring the state to the allocation order
+                    v = np.ascontiguousarray(v.reshape((2,) * qubits).transpose(
+                        relayout_axes(dict(m), ident, qubits))).reshape(-1)
+                states[key] = v
         out[key + "_ms"] = min(times)
         del sim
-    a = states["c128_tc"]
+    ref = OracleSimulator(7, qubits, cluster)
+    ref.allocate_qureg(qs, 0)
+    circuits.replay(ref, cmds)
+    ref.run()
+    a = ref.vec
+    c128 = states.pop("c128_tc")
+    out["c128_tc_max_abs_error"] = float(np.max(np.abs(c128 - a)))
+    del c128
     for key, _, _ in modes[1:]:
-        b = states.pop(key)
+        b = states.pop(key).astype(np.complex128)
         nb = float(np.vdot(b, b).real)
         ov = float(abs(np.vdot(a, b)) ** 2)
         ms = out.pop(key + "_ms")
         out[key] = {"ms": ms, "fidelity": ov, "fidelity_normalized": ov / nb, "norm": nb,
                     "max_abs_error": float(np.max(np.abs(a - b))), "speedup_over_c128": out["c128_tc_ms"] / ms}
-        log("precision %s: fidelity %.3e below 1 (normalized %.3e), norm-1 %.2e, %.0f ms vs c128 %.0f ms" % (
-            key, 1 - ov, 1 - ov / nb, nb - 1, out[key]["ms"], out["c128_tc_ms"]))
+        log("precision %s: fidelity %.3e below 1 (normalized %.3e), norm-1 %.2e, max err %.2e, %.0f ms vs c128 %.0f ms" % (
+            key, 1 - ov, 1 - ov / nb, nb - 1, out[key]["max_abs_error"], out[key]["ms"], out["c128_tc_ms"]))
+        del b
+    log("precision c128_tc: max err vs oracle %.2e" % out["c128_tc_max_abs_error"])
+    del ref, a
     return out
+
+
+# ------------------------------------------------------------ parity legs
+# The oracle (oracle/, the C restatement of the reference engine, OpenMP on
+# the host cores) is the checker here: the product's states, expectation
+# values and samples are compared with it on the configurations the metric
+# is quoted on. Nothing measured above runs through it.
+
+def relayout_axes(map_src, map_dst, n):
+    """Axes that transpose a state stored in layout map_src (qubit id -> bit
+    position), viewed as shape (2,)*n (axis k = bit n-1-k), into layout
+    map_dst."""
+    axes = [0] * n
+    for q, pd in map_dst.items():
+        axes[n - 1 - pd] = n - 1 - map_src[q]
+    return axes
+
+
+def max_abs_diff(a, map_a, b, map_b, n, chunk_axes=6):
+    """max |a - b| over every amplitude; a in layout map_a, b in layout
+    map_b, compared in 2^chunk_axes chunks of b's order."""
+    A = a.reshape((2,) * n).transpose(relayout_axes(map_a, map_b, n))
+    c = min(chunk_axes, n)
+    B = b.reshape((1 << c, -1))
+    worst = 0.0
+    for k in range(1 << c):
+        idx = tuple((k >> (c - 1 - t)) & 1 for t in range(c))
+        blk = np.ascontiguousarray(A[idx]).reshape(-1)
+        worst = max(worst, float(np.max(np.abs(blk - B[k]))))
+    return worst
+
+
+def remap_indices(idx, map_src, map_dst):
+    """Basis indices in layout map_src rewritten for layout map_dst."""
+    idx = np.asarray(idx, dtype=np.uint64)
+    out = np.zeros_like(idx)
+    for q, ps in map_src.items():
+        out |= ((idx >> np.uint64(ps)) & np.uint64(1)) << np.uint64(map_dst[q])
+    return out
+
+
+def parity_headline(args, cmds, zz, shots):
+    """The benchmark configuration at full size against the oracle: the
+    fused circuit (QFT + 10 random layers, greedy k <= 5) on the GPU and on
+    the oracle; every amplitude compared (max-abs <= 1e-12); the 1024 seeded
+    full-register samples (same MT19937 draws; identical wherever the draw's
+    distance to the deciding CDF boundary exceeds 1e-12, the others counted);
+    the forced permutation (2^22 seeded amplitudes followed bit-exactly to
+    their new positions, then every amplitude against the oracle again); the
+    64 <Z_i Z_j> after it (<= 1e-11)."""
+    import hiqsimulator_gb300 as hqs
+    from hiqsimulator_gb300 import circuits
+    from oracle.engine import OracleSimulator
+    n = N_QUBITS
+    ids = list(range(n))
+    out = {"qubits": n, "tolerances": {"amplitudes_max_abs": 1e-12, "zz_abs": 1e-11, "sample_margin": 1e-12}}
+    t0 = time.perf_counter()
+    sim = hqs.SimulatorMPI(SEED, n, CLUSTER, "c128", args.arith)
+    sim.set_pass_limits(defer=args.defer)
+    sim.allocate_qureg(ids, 0)
+    circuits.replay(sim, cmds)
+    sim.run()
+    sim.synchronize()
+    ref = OracleSimulator(SEED, n, CLUSTER)
+    ref.allocate_qureg(ids, 0)
+    t1 = time.perf_counter()
+    circuits.replay(ref, cmds)
+    ref.run()
+    out["oracle_seconds"] = time.perf_counter() - t1
+    rmap, rvec = {q: p for p, q in enumerate(ref.get_qubits_ids())}, ref.vec
+    gmap, gvec = sim.cheat_local_numpy()
+    gmap = dict(gmap)
+    out["layout_equal_before_permutation"] = gmap == rmap
+    out["amplitudes_max_abs"] = max_abs_diff(gvec, gmap, rvec, rmap, n)
+    # seeded amplitudes to follow through the permutation
+    pick = np.random.default_rng(SEED).integers(0, 1 << n, size=1 << 22, dtype=np.uint64)
+    before = gvec[pick.astype(np.int64)].copy()
+    del gvec
+    # samples: the same draws on both sides
+    got = remap_indices(np.asarray(sim.sample(shots), dtype=np.uint64), gmap, rmap).astype(np.int64)
+    rnds = np.array([ref.rng.uniform() for _ in range(shots)])
+    want, margin = ref.sample_many(rnds)
+    decided = margin > 1e-12
+    out["samples"] = {"shots": shots, "compared": int(decided.sum()),
+                      "mismatches": int(np.sum((got != want) & decided)),
+                      "near_ties": int((~decided).sum()), "near_tie_mismatches": int(np.sum((got != want) & ~decided)),
+                      "distinct": int(len(np.unique(got))), "min_margin": float(margin.min())}
+    # the forced permutation
+    force_permutation(sim)
+    pmap, pvec = sim.cheat_local_numpy()
+    pmap = dict(pmap)
+    moved = remap_indices(pick, gmap, pmap).astype(np.int64)
+    out["permutation"] = {"followed_amplitudes": int(len(pick)),
+                          "bit_exact": bool(np.array_equal(pvec[moved].view(np.uint64), before.view(np.uint64))),
+                          "layout_changed": pmap != gmap,
+                          "amplitudes_max_abs_vs_oracle": max_abs_diff(pvec, pmap, rvec, rmap, n)}
+    del pvec, before
+    zg = [sim.get_expectation_value([([(a, "Z"), (b, "Z")], 1.0)], ids) for a, b in zz]
+    zr = [ref.get_expectation_value([([(a, "Z"), (b, "Z")], 1.0)], ids) for a, b in zz]
+    out["zz"] = {"pairs": len(zz), "max_abs": float(np.max(np.abs(np.array(zg) - np.array(zr))))}
+    out["norm_minus_1"] = sim.get_probability([], []) - 1.0
+    out["pass"] = bool(out["amplitudes_max_abs"] <= 1e-12 and out["permutation"]["bit_exact"]
+                       and out["permutation"]["amplitudes_max_abs_vs_oracle"] <= 1e-12
+                       and out["samples"]["mismatches"] == 0 and out["zz"]["max_abs"] <= 1e-11)
+    out["seconds"] = time.perf_counter() - t0
+    del sim, ref, rvec
+    log("parity %dq: amplitudes %.2e, permuted %.2e (bit-exact %s), samples %d/%d compared, %d mismatches, "
+        "zz %.2e, oracle %.0f s -> %s" % (n, out["amplitudes_max_abs"], out["permutation"]["amplitudes_max_abs_vs_oracle"],
+                                          out["permutation"]["bit_exact"], out["samples"]["compared"], shots,
+                                          out["samples"]["mismatches"], out["zz"]["max_abs"], out["oracle_seconds"],
+                                          "pass" if out["pass"] else "FAIL"))
+    return out
+
+
+def parity_20q():
+    """The 20-qubit random circuit (20 layers as in the benchmark's random
+    layers), fusion off and greedy k <= 4: all 2^20 amplitudes and the 20
+    single-qubit P(1) against the oracle."""
+    import hiqsimulator_gb300 as hqs
+    from hiqsimulator_gb300 import circuits
+    from oracle.engine import OracleSimulator
+    n = 20
+    qs = list(range(n))
+    gates = circuits.random_circuit_20q(seed=1234, n=n, layers=20)
+    out = {}
+    for mode, cmds in (("fusion_off", circuits.fusion_off_stream(gates)),
+                       ("greedy_k4", circuits.greedy_stream(gates, qs, 4))):
+        ref = OracleSimulator(1234, n, 4)
+        sim = hqs.SimulatorMPI(1234, n, 4, "c128")
+        for s in (ref, sim):
+            s.allocate_qureg(qs, 0)
+            circuits.replay(s, cmds)
+            s.run()
+        gmap, gvec = sim.cheat_local_numpy()
+        rmap = {q: p for p, q in enumerate(ref.get_qubits_ids())}
+        p1 = max(abs(sim.get_probability([True], [q]) - ref.get_probability([True], [q])) for q in qs)
+        out[mode] = {"amplitudes": 1 << n, "amplitudes_max_abs": max_abs_diff(gvec, dict(gmap), ref.vec, rmap, n),
+                     "p1_max_abs": float(p1)}
+        out[mode]["pass"] = bool(out[mode]["amplitudes_max_abs"] <= 1e-12 and p1 <= 1e-12)
+        log("parity 20q %s: amplitudes %.2e, P(1) %.2e" % (mode, out[mode]["amplitudes_max_abs"], p1))
+        del sim, ref
+    return out
+
+
+def parity_report(args, cmds, zz, shots):
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    out = {"checker": "oracle/ (C restatement of the reference engine, pinned to the reference's own outputs)",
+           "host_threads": int(os.environ["OMP_NUM_THREADS"])}
+    out["random_20q"] = parity_20q()
+    out["headline_%dq" % N_QUBITS] = parity_headline(args, cmds, zz, shots)
+    return out
+
+
+def run_tour(args):
+    """One launch or a few of every state-streaming kernel on an
+    args.qubits-qubit state (the workload for the per-kernel ncu summaries):
+    fused passes of the benchmark circuit in tensor-core digit mode and in
+    double-float mode, probability, the measurement block sums, Z-string and
+    general Pauli expectation values, the qubit permutation, collapse, the
+    drop of a qubit and one batched serving round."""
+    import hiqsimulator_gb300 as hqs
+    from hiqsimulator_gb300 import circuits, serving
+    n = N_QUBITS
+    ids = list(range(n))
+    gates = circuits.qft_random_layers(seed=SEED, n=n, layers=2)
+    cmds = circuits.greedy_stream(gates, ids, CLUSTER)
+    head = []
+    runs = 0
+    for c in cmds:
+        head.append(c)
+        runs += c[0] == "run"
+        if runs == 24:
+            break
+    def replayed(arith):
+        sim = hqs.SimulatorMPI(SEED, n, CLUSTER, "c128", arith)
+        sim.allocate_qureg(ids, 0)
+        circuits.replay(sim, head)
+        sim.run()
+        sim.synchronize()
+        log("tour %s: %d fused gates" % (arith, runs))
+        return sim
+
+    sim = replayed("df")
+    del sim
+    sim = replayed("tc")
+    p = sim.get_probability([True], [3])
+    smp = sim.sample(64)
+    zz = sim.get_expectation_value([([(2, "Z"), (n - 1, "Z")], 1.0)], ids)
+    xy = sim.get_expectation_value([([(0, "X"), (5, "Y")], 0.5), ([(7, "Z")], 0.25)], ids)
+    force_permutation(sim)
+    sim.collapse_wavefunction([n - 1], [p > 0.5])
+    sim.deallocate_qubit(n - 1)
+    sim.synchronize()
+    log("tour queries: p %.3f, %d samples, zz %.3e, xy %.3e" % (p, len(smp), zz, xy))
+    del sim
+    work = serving.serving_workload(11, 24)
+    res, st = serving.serve(work, np.zeros(len(work)), precision="c128", arith="tc", budget_bytes=8e9, max_active=24)
+    log("tour serving: %d circuits, %d launches" % (len(res), st["launches"]))
+    return 0
 
 
 def run_reference(args, dist):
@@ -501,13 +721,33 @@ def run_ours(args, dist):
     peak, peak_kind = measured_peak()
     nl = max(pt["launches"], 1)
     algo = args.steps * pass_ref_bytes
+    kinds = {}
+    for kname, nops, byts, lms in pt["log"]:
+        k = kinds.setdefault(kname, {"launches": 0, "bytes": 0, "ms": 0.0, "ops": 0})
+        k["launches"] += 1
+        k["bytes"] += byts
+        k["ms"] += lms
+        k["ops"] += nops
+    for k in kinds.values():
+        k["GBs"] = k["bytes"] / (k["ms"] / 1e3) / 1e9 if k["ms"] > 0 else 0.0
+        k["frac"] = k["GBs"] / peak
+        k["avg_launch_ms"] = k["ms"] / max(k["launches"], 1)
+        k["share"] = k["ms"] / pt["ms"] if pt["ms"] > 0 else 0.0
+    top = max(kinds, key=lambda x: kinds[x]["ms"]) if kinds else "pass_kernel"
+    for kname, k in sorted(kinds.items()):
+        log("kernel %s: %d launches, %.1f ms avg, %.0f GB/s sweep (%.3f of %s HBM), %.0f%% of pass time" % (
+            kname, k["launches"], k["avg_launch_ms"], k["GBs"], k["frac"], peak_kind, 100 * k["share"]))
     sweep = pt["bytes"] / (pt["ms"] / 1e3) / 1e9 if pt["ms"] > 0 else 0.0
     refeq = algo / (pt["ms"] / 1e3) / 1e9 if pt["ms"] > 0 else 0.0
-    traffic = profile_traffic()
-    roof = {"bound": "hbm", "achieved": sweep, "peak": peak, "unit": "GB/s", "frac": sweep / peak,
-            "traffic": traffic, "peak_source": peak_kind, "kernel": "pass_kernel<%s>" % sim.arith,
-            "launches": pt["launches"], "algorithmic_bytes_per_launch": pt["bytes"] / nl,
-            "avg_launch_ms": pt["ms"] / nl, "fused_gates_per_launch": args.steps * len(clusters) / nl,
+    traffic = profile_traffic(top)
+    kt = kinds.get(top, {"GBs": sweep, "launches": nl, "bytes": pt["bytes"], "ms": pt["ms"]})
+    roof = {"bound": "hbm", "achieved": kt["GBs"], "peak": peak, "unit": "GB/s", "frac": kt["GBs"] / peak,
+            "traffic": traffic, "peak_source": peak_kind, "kernel": top,
+            "launches": kt["launches"], "algorithmic_bytes_per_launch": kt["bytes"] / max(kt["launches"], 1),
+            "avg_launch_ms": kt["ms"] / max(kt["launches"], 1),
+            "all_pass_launches": {"launches": pt["launches"], "GBs": sweep, "frac": sweep / peak,
+                                  "fused_gates_per_launch": args.steps * len(clusters) / nl},
+            "kernels": kinds,
             "reference_equivalent_bytes_per_launch": algo / nl, "reference_equivalent_GBs": refeq,
             "reference_equivalent_frac": refeq / peak}
     # the same launches against GB300's FP64 rate: the reference's FP64 flops
@@ -555,6 +795,7 @@ def run_ours(args, dist):
 
     serv = serving_report(args) if (dist.rank == 0 and args.serve > 0) else None
     prec = precision_report() if (dist.rank == 0 and not args.no_precision) else None
+    par = parity_report(args, cmds, zz, shots) if (dist.rank == 0 and not args.no_parity) else None
     cap = capacity_report() if (dist.rank == 0 and args.capacity) else None
     table = table_report(cmds, pass_ref_bytes) if (dist.rank == 0 and args.table) else None
 
@@ -570,7 +811,7 @@ def run_ours(args, dist):
                            "state_bytes": 16 << N_QUBITS, "l2": "inputs larger than L2 (%d MiB state)" % ((16 << N_QUBITS) >> 20),
                            "parallelism": "replicas" if dist.ws > 1 else "single GPU"},
                 "roofline": roof, "fp64_roofline": roof64, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
-                "clocks": clk, "serving": serv, "precision": prec, "capacity": cap, "table": table}
+                "clocks": clk, "parity": par, "serving": serv, "precision": prec, "capacity": cap, "table": table}
         print(json.dumps(line), flush=True)
     return 0
 
@@ -604,6 +845,8 @@ def main():
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[4000.0, 400.0])
     ap.add_argument("--serve-slots", type=int, default=32, help="resident circuits at most while serving")
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the comparisons with the oracle")
+    ap.add_argument("--tour", action="store_true", help="launch every state-streaming kernel once (profiling)")
     ap.add_argument("--capacity", action="store_true", help="also run the 33q c128 / 34q c64 capacity states")
     ap.add_argument("--table", action="store_true", help="also time the reference-against-GPU table rows")
     args = ap.parse_args()
@@ -614,6 +857,8 @@ def main():
     try:
         if args.impl == "reference":
             return run_reference(args, dist)
+        if args.tour:
+            return run_tour(args)
         return run_ours(args, dist)
     finally:
         dist.close()

@@ -23,6 +23,7 @@ struct hqs_sim {
     hqs::Engine* eng = nullptr;
     std::string err;
     cudaEvent_t t0 = nullptr, t1 = nullptr;
+    std::vector<hqs::Workspace::LaunchRecord> pass_log;  // launches of the last pass_timing call
 };
 
 struct hqs_server {
@@ -371,10 +372,25 @@ int hqs_sim_set_pass_timing(hqs_sim* sim, int on) {
 int hqs_sim_pass_timing(hqs_sim* sim, uint64_t* launches, uint64_t* bytes, double* ms) {
     SIM_CALL(sim, {
         sim->eng->flush();
-        const hqs::Workspace::PassTiming t = sim->eng->workspace().collect_timing();
+        hqs::Workspace::PassTiming t = sim->eng->workspace().collect_timing();
         if (launches) *launches = t.launches;
         if (bytes) *bytes = t.bytes;
         if (ms) *ms = t.ms;
+        sim->pass_log = std::move(t.log);
+    });
+}
+
+int hqs_sim_pass_log(hqs_sim* sim, hqs_pass_record* out, size_t cap, size_t* count) {
+    SIM_CALL(sim, {
+        need(count != nullptr && (cap == 0 || out != nullptr), "hqs_sim_pass_log: null output");
+        *count = sim->pass_log.size();
+        for (size_t i = 0; i < std::min(cap, sim->pass_log.size()); ++i) {
+            const auto& r = sim->pass_log[i];
+            out[i].kernel = r.kind;
+            out[i].nops = r.nops;
+            out[i].bytes = r.bytes;
+            out[i].ms = r.ms;
+        }
     });
 }
 

@@ -301,6 +301,15 @@ public:
         d["launches"] = launches;
         d["bytes"] = bytes;
         d["ms"] = ms;
+        size_t cnt = 0;
+        check(hqs_sim_pass_log(h_, nullptr, 0, &cnt));
+        std::vector<hqs_pass_record> rec(cnt);
+        if (cnt) check(hqs_sim_pass_log(h_, rec.data(), cnt, &cnt));
+        py::list log;
+        for (const auto& r : rec)
+            log.append(py::make_tuple(r.kernel == HQS_KERNEL_UMMA ? "umma_pass_kernel" : "pass_kernel", r.nops,
+                                      r.bytes, r.ms));
+        d["log"] = log;
         return d;
     }
     // Zero-copy export of the device state (position order) as a DLPack

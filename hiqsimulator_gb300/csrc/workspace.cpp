@@ -835,8 +835,10 @@ uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<G
         cuda_check(cudaEventRecord(staging_free_, stream_), "cudaEventRecord");
         staging_pending_ = true;
         uint64_t bytes = 0;
-        for (const auto& l : L) {
-            TimedLaunch tl{nullptr, nullptr, l.bytes};
+        for (size_t li = 0; li < L.size(); ++li) {
+            const auto& l = L[li];
+            const size_t lend = li + 1 < L.size() ? L[li + 1].first : ops.size();
+            TimedLaunch tl{nullptr, nullptr, l.bytes, l.umma ? 1 : 0, (int)(lend - l.first)};
             if (timing_) {
                 tl.a = take_event();
                 tl.b = take_event();
@@ -873,8 +875,10 @@ uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<G
     cuda_check(cudaEventRecord(staging_free_, stream_), "cudaEventRecord");
     staging_pending_ = true;
     uint64_t bytes = 0;
-    for (const auto& p : plans) {
-        TimedLaunch tl{nullptr, nullptr, p.bytes};
+    for (size_t pi = 0; pi < plans.size(); ++pi) {
+        const PassPlan& p = plans[pi];
+        const size_t pend = pi + 1 < plans.size() ? first[pi + 1] : ops.size();
+        TimedLaunch tl{nullptr, nullptr, p.bytes, 0, (int)(pend - first[pi])};
         if (timing_) {
             tl.a = take_event();
             tl.b = take_event();
@@ -912,6 +916,7 @@ Workspace::PassTiming Workspace::collect_timing() {
         t.ms += ms;
         t.bytes += tl.bytes;
         ++t.launches;
+        t.log.push_back({tl.kind, tl.nops, tl.bytes, (double)ms});
         event_pool_.push_back(tl.a);
         event_pool_.push_back(tl.b);
     }

@@ -70,10 +70,17 @@ public:
     // Per-launch device timing of the apply passes (CUDA events around each
     // launch on the workspace stream). collect_timing() waits for the events,
     // returns the totals since the last collection and clears them.
+    struct LaunchRecord {
+        int kind = 0;  // 0: pass kernel, 1: tensor-memory pass
+        int nops = 0;  // gate ops the launch applies
+        uint64_t bytes = 0;
+        double ms = 0.0;
+    };
     struct PassTiming {
         uint64_t launches = 0;
         uint64_t bytes = 0;
         double ms = 0.0;
+        std::vector<LaunchRecord> log;  // one record per launch, in launch order
     };
     void set_timing(bool on) { timing_ = on; }
     PassTiming collect_timing();
@@ -98,6 +105,7 @@ private:
     struct TimedLaunch {
         cudaEvent_t a, b;
         uint64_t bytes;
+        int kind, nops;
     };
     std::vector<TimedLaunch> timed_;
     std::vector<cudaEvent_t> event_pool_;

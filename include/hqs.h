@@ -172,6 +172,19 @@ int hqs_sim_timer_stop(hqs_sim* sim, float* ms);
  * the previous call. */
 int hqs_sim_set_pass_timing(hqs_sim* sim, int on);
 int hqs_sim_pass_timing(hqs_sim* sim, uint64_t* launches, uint64_t* bytes, double* ms);
+/* The launches behind the last hqs_sim_pass_timing call, in launch order:
+ * kernel (HQS_KERNEL_PASS: the tiled pass kernel; HQS_KERNEL_UMMA: the
+ * tensor-memory pass), gate ops applied, algorithmic HBM bytes and device
+ * milliseconds. Up to cap records are written; *count receives the total. */
+#define HQS_KERNEL_PASS 0
+#define HQS_KERNEL_UMMA 1
+typedef struct {
+    int32_t kernel;
+    int32_t nops;
+    uint64_t bytes;
+    double ms;
+} hqs_pass_record;
+int hqs_sim_pass_log(hqs_sim* sim, hqs_pass_record* out, size_t cap, size_t* count);
 
 /* Greedy fusion schedule (the rule of HiQ's GreedyScheduler + ClusterScheduler,
  * hiq/projectq/cengines/_greedyscheduler.py:119-137,

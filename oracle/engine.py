@@ -252,6 +252,16 @@ class OracleSimulator:
         self.last_margin = margin.value
         return idx
 
+    def sample_many(self, rnds):
+        """sample_index for every draw of rnds on the current state (one
+        block CDF): (indices, margins) as int64 / float64 arrays."""
+        r = np.ascontiguousarray(rnds, dtype=np.float64)
+        idx = np.zeros(len(r), dtype=np.int64)
+        mar = np.zeros(len(r), dtype=np.float64)
+        self.lib.orc_sample_many(dptr(self.vec.view(np.float64)), len(self.vec), len(r), dptr(r),
+                                 idx.ctypes.data_as(ctypes.POINTER(ctypes.c_int64)), dptr(mar))
+        return idx, mar
+
     def measure_qubits(self, ids):
         """SimulatorMPI.cpp:897-1008."""
         rnd = self.rng.uniform()

@@ -50,6 +50,7 @@ def load_oracle_lib():
         lib.orc_block_cdf.argtypes = [_dp, ctypes.c_uint64, ctypes.c_uint64, _dp]
         lib.orc_sample_index.argtypes = [_dp, ctypes.c_uint64, ctypes.c_double, _dp]
         lib.orc_sample_index.restype = ctypes.c_int64
+        lib.orc_sample_many.argtypes = [_dp, ctypes.c_uint64, ctypes.c_int64, _dp, _i64p, _dp]
         lib.orc_bit_probs.argtypes = [_dp, ctypes.c_uint64, ctypes.c_uint, _dp]
         lib.orc_drop_bit.argtypes = [_dp, ctypes.c_uint64, ctypes.c_uint, ctypes.c_int]
         lib.orc_entropy.argtypes = [_dp, ctypes.c_uint64]

@@ -146,20 +146,18 @@ void orc_block_cdf(const double* psi_d, uint64_t n_amps, uint64_t nblocks, doubl
     for (uint64_t b = 1; b < nblocks; ++b) out[b] += out[b - 1];
 }
 
-/* Sampled basis index for one uniform draw rnd (MeasureQubits,
- * SimulatorMPI.cpp:897-964): first block whose CDF reaches rnd, then a serial
- * scan inside it until the running sum reaches rnd. Returns -1 when rnd exceeds
- * the total (the reference throws there). margin_out receives the smallest
- * distance between rnd and a CDF boundary that decided the outcome. */
-int64_t orc_sample_index(const double* psi_d, uint64_t n_amps, double rnd, double* margin_out) {
-    const cplx* psi = (const cplx*)psi_d;
-    uint64_t nb = n_amps < (1ULL << 15) ? n_amps : (1ULL << 15);
-    double* cdf = (double*)malloc(sizeof(double) * nb);
-    orc_block_cdf(psi_d, n_amps, nb, cdf);
+/* Sampled basis index for one uniform draw rnd given the block CDF cdf[nb]
+ * (MeasureQubits, SimulatorMPI.cpp:897-964): first block whose CDF reaches
+ * rnd, then a serial scan inside it until the running sum reaches rnd.
+ * Returns -1 when rnd exceeds the total (the reference throws there).
+ * margin_out receives the smallest distance between rnd and a CDF boundary
+ * that decided the outcome. */
+static int64_t sample_in_cdf(const cplx* psi, uint64_t n_amps, const double* cdf, uint64_t nb, double rnd,
+                             double* margin_out) {
     uint64_t i = 0;
     for (; i < nb; ++i)
         if (rnd <= cdf[i]) break;
-    if (i == nb) { free(cdf); return -1; }
+    if (i == nb) return -1;
     double margin = fabs(cdf[i] - rnd);
     if (i > 0 && fabs(rnd - cdf[i - 1]) < margin) margin = fabs(rnd - cdf[i - 1]);
     uint64_t K = n_amps / nb;
@@ -176,9 +174,32 @@ int64_t orc_sample_index(const double* psi_d, uint64_t n_amps, double rnd, doubl
         }
     }
     /* the reference leaves k one past the block when the scan never reaches rnd */
-    free(cdf);
     if (margin_out) *margin_out = margin;
     return (int64_t)k;
+}
+
+static uint64_t sample_blocks(uint64_t n_amps) { return n_amps < (1ULL << 15) ? n_amps : (1ULL << 15); }
+
+int64_t orc_sample_index(const double* psi_d, uint64_t n_amps, double rnd, double* margin_out) {
+    uint64_t nb = sample_blocks(n_amps);
+    double* cdf = (double*)malloc(sizeof(double) * nb);
+    orc_block_cdf(psi_d, n_amps, nb, cdf);
+    int64_t k = sample_in_cdf((const cplx*)psi_d, n_amps, cdf, nb, rnd, margin_out);
+    free(cdf);
+    return k;
+}
+
+/* orc_sample_index for nrnd draws of one state: the block CDF once, then one
+ * scan per draw (the state does not change between the draws). */
+void orc_sample_many(const double* psi_d, uint64_t n_amps, int64_t nrnd, const double* rnd, int64_t* idx_out,
+                     double* margin_out) {
+    uint64_t nb = sample_blocks(n_amps);
+    double* cdf = (double*)malloc(sizeof(double) * nb);
+    orc_block_cdf(psi_d, n_amps, nb, cdf);
+#pragma omp parallel for schedule(dynamic, 4)
+    for (int64_t r = 0; r < nrnd; ++r)
+        idx_out[r] = sample_in_cdf((const cplx*)psi_d, n_amps, cdf, nb, rnd[r], &margin_out[r]);
+    free(cdf);
 }
 
 /* P(bit pos = 0) and P(bit pos = 1) (DeallocateLocalQubit, SimulatorMPI.cpp:283-287). */

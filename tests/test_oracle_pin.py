@@ -103,6 +103,26 @@ def test_oracle_rng_matches_reference():
         assert got == outs, seed
 
 
+def test_oracle_sample_many_matches_single_draws():
+    """One block CDF for many draws gives the index and margin of a
+    separate sample_index per draw (the draws that decide measure_qubits),
+    including draws on block boundaries and a draw above the total."""
+    rng = np.random.default_rng(8)
+    for n in (6, 17):
+        sim = OracleSimulator(3, 24, 4)
+        sim.allocate_qureg(list(range(n)), 0)
+        v = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+        v[rng.random(1 << n) < 0.2] = 0
+        sim.vec = v / np.linalg.norm(v)
+        cdf = np.cumsum(np.abs(sim.vec) ** 2)
+        rnds = np.concatenate([rng.random(200), cdf[[0, 5, len(cdf) // 3]], [1.5]])
+        idx, mar = sim.sample_many(rnds)
+        for r, i, m in zip(rnds, idx, mar):
+            assert sim.sample_index(float(r)) == i
+            if i >= 0:
+                assert sim.last_margin == m
+
+
 def test_oracle_errors_match_reference():
     ref = json.load(open(os.path.join(GOLDEN, "ref_errors.json")))
     sim = OracleSimulator(1, 20, 4)
