@@ -635,8 +635,10 @@ def run_tour(args):
     zz = sim.get_expectation_value([([(2, "Z"), (n - 1, "Z")], 1.0)], ids)
     xy = sim.get_expectation_value([([(0, "X"), (5, "Y")], 0.5), ([(7, "Z")], 0.25)], ids)
     force_permutation(sim)
-    sim.collapse_wavefunction([n - 1], [p > 0.5])
-    sim.deallocate_qubit(n - 1)
+    low = sim.get_qubits_ids()[0]  # the qubit now at position 0: dropping it compacts the whole state
+    p0 = sim.get_probability([True], [low])
+    sim.collapse_wavefunction([low], [p0 > 0.5])
+    sim.deallocate_qubit(low)
     sim.synchronize()
     log("tour queries: p %.3f, %d samples, zz %.3e, xy %.3e" % (p, len(smp), zz, xy))
     del sim

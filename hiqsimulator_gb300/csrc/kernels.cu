@@ -1008,8 +1008,19 @@ __global__ void __launch_bounds__(kThreads) bit_probs_kernel(const S* __restrict
                                                              double* __restrict__ partials) {
     __shared__ double red[64];
     NA a0, a1;
-    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
-         i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < count; i += 4 * stride) {  // four amplitudes in flight per thread
+        S v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = state[i + u * stride];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            if (((i + u * stride) >> pos) & 1ULL) a1.add(v[u]);
+            else a0.add(v[u]);
+        }
+    }
+    for (; i < count; i += stride) {
         if ((i >> pos) & 1ULL) a1.add(state[i]);
         else a0.add(state[i]);
     }
@@ -1046,7 +1057,15 @@ __global__ void __launch_bounds__(kThreads) block_sum_cta_kernel(const S* __rest
     __shared__ double red[32];
     NA acc;
     const uint64_t b0 = (uint64_t)blockIdx.x * K;
-    for (uint64_t j = threadIdx.x; j < K; j += blockDim.x) acc.add(state[b0 + j]);
+    uint64_t j = threadIdx.x;
+    for (; j + 3 * kThreads < K; j += 4 * kThreads) {  // four amplitudes in flight per thread
+        S v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = state[b0 + j + u * kThreads];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc.add(v[u]);
+    }
+    for (; j < K; j += kThreads) acc.add(state[b0 + j]);
     double v[1] = {acc.value()};
     block_sum<1>(v, red);
     if (threadIdx.x == 0) out[blockIdx.x] = v[0];
@@ -1135,6 +1154,27 @@ __global__ void __launch_bounds__(kThreads) zparity_kernel(const S* __restrict__
     if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
 }
 
+// One term of a Pauli sum as the expectation kernel uses it: x the flip
+// mask, yz the sign mask, h the lowest bit of x (an unordered pair {i, i^x}
+// is visited from its member with bit h clear), im whether the pair
+// contributes through Im(conj(a_i) a_j) (an odd number of sign bits inside
+// x) rather than the real part, k the real weight as a double-float.
+struct PauliTermDev {
+    uint64_t x, yz;
+    float kh, kl;
+    int h, im;
+};
+constexpr int kPauliChunk = 64;
+
+// sum_t Re(w_t sum_i conj(a_i) ph_t(i ^ x_t) a_(i ^ x_t)), ph_t(k) =
+// (-1)^popcount(k & (Y_t | Z_t)), w_t = c_t i^|Y_t|, in one read of the
+// state per chunk of 64 terms: each amplitude is loaded once, a term with
+// x_t = 0 adds Re(w_t) ph_t(i) |a_i|^2, a term with x_t != 0 takes each pair
+// {i, j = i ^ x_t} once. With P = conj(a_i) a_j and s_i = ph_t(i), the pair
+// adds Re(w (s_j P + s_i conj(P))) = 2 s_i Re(w) Re(P) when s_i = s_j and
+// 2 s_i Im(w) Im(P) when s_i = -s_j (s_i s_j = (-1)^popcount(x_t & yz_t)
+// is the same for every pair of the term). Products and sums in
+// double-float.
 template <class S>
 __global__ void __launch_bounds__(kThreads) pauli_expect_kernel(const S* __restrict__ state, uint64_t count,
                                                                 int nterms, const uint64_t* __restrict__ xm,
@@ -1143,44 +1183,79 @@ __global__ void __launch_bounds__(kThreads) pauli_expect_kernel(const S* __restr
                                                                 const double* __restrict__ coef,
                                                                 double* __restrict__ partials) {
     __shared__ double red[32];
-    double total = 0.0;
-    for (int t = 0; t < nterms; ++t) {
-        const uint64_t x = xm[t], yz = ym[t] | zm[t];
-        const int ny = __popcll(ym[t]) & 3;
-        NormAccDF sre, sim;  // double-float accumulators of the real / imaginary sums
+    __shared__ PauliTermDev tm[kPauliChunk];
+    float acc_h = 0.f, acc_l = 0.f;
+    auto add = [&](float vh, float vl, const PauliTermDev& T, bool neg) {
+        // (vh + vl) (kh + kl), negated when the sign is odd, into the accumulator
+        float p = vh * T.kh;
+        float e = fmaf(vh, T.kh, -p);
+        e = fmaf(vh, T.kl, fmaf(vl, T.kh, e));
+        if (neg) {
+            p = -p;
+            e = -e;
+        }
+        const float s = acc_h + p, bb = s - acc_h;
+        acc_l += ((acc_h - (s - bb)) + (p - bb)) + e;
+        acc_h = s;
+    };
+    for (int t0 = 0; t0 < nterms; t0 += kPauliChunk) {
+        const int tn = min(kPauliChunk, nterms - t0);
+        __syncthreads();
+        if (threadIdx.x < tn) {
+            const int t = t0 + threadIdx.x;
+            PauliTermDev T;
+            T.x = xm[t];
+            T.yz = ym[t] | zm[t];
+            double wr = coef[2 * t], wi = coef[2 * t + 1];
+            for (int r = 0; r < (__popcll(ym[t]) & 3); ++r) {  // w = c i^|Y|
+                const double tr = -wi;
+                wi = wr;
+                wr = tr;
+            }
+            double k = wr;
+            T.im = 0;
+            T.h = 0;
+            if (T.x != 0) {
+                T.im = __popcll(T.x & T.yz) & 1;
+                k = 2.0 * (T.im ? wi : wr);
+                T.h = __ffsll((long long)T.x) - 1;
+            }
+            const DF kd = df_split(k);
+            T.kh = kd.h;
+            T.kl = kd.l;
+            tm[threadIdx.x] = T;
+        }
+        __syncthreads();
         for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < count;
              i += (uint64_t)gridDim.x * blockDim.x) {
-            const uint64_t j = i ^ x;
-            double ar, ai, br, bi;
+            double ar, ai;
             load_d2<S>(state, i, ar, ai);
-            load_d2<S>(state, j, br, bi);
-            if (__popcll(j & yz) & 1) { br = -br; bi = -bi; }
-            // conj(a) * b = (ar br + ai bi) + i (ar bi - ai br), each product split exactly
-            const DF arf = df_split(ar), aif = df_split(ai), brf = df_split(br), bif = df_split(bi);
-            float rh = 0.f, rl = 0.f, ih = 0.f, il = 0.f;
-            df_mac(rh, rl, arf.h, arf.l, brf.h, brf.l);
-            df_mac(rh, rl, aif.h, aif.l, bif.h, bif.l);
-            df_mac(ih, il, arf.h, arf.l, bif.h, bif.l);
-            df_mac(ih, il, -aif.h, -aif.l, brf.h, brf.l);
-            // accumulate (rh + rl) and (ih + il)
-            float s = sre.h + rh, bb = s - sre.h;
-            sre.l += ((sre.h - (s - bb)) + (rh - bb)) + rl;
-            sre.h = s;
-            s = sim.h + ih;
-            bb = s - sim.h;
-            sim.l += ((sim.h - (s - bb)) + (ih - bb)) + il;
-            sim.h = s;
+            const DF arf = df_split(ar), aif = df_split(ai);
+            for (int t = 0; t < tn; ++t) {
+                const PauliTermDev T = tm[t];
+                const bool neg = (__popcll(i & T.yz) & 1) != 0;
+                float vh = 0.f, vl = 0.f;
+                if (T.x == 0) {
+                    df_mac(vh, vl, arf.h, arf.l, arf.h, arf.l);
+                    df_mac(vh, vl, aif.h, aif.l, aif.h, aif.l);
+                } else {
+                    if ((i >> T.h) & 1ULL) continue;
+                    double br, bi;
+                    load_d2<S>(state, i ^ T.x, br, bi);
+                    const DF brf = df_split(br), bif = df_split(bi);
+                    if (T.im) {  // Im(conj(a) b) = ar bi - ai br
+                        df_mac(vh, vl, arf.h, arf.l, bif.h, bif.l);
+                        df_mac(vh, vl, -aif.h, -aif.l, brf.h, brf.l);
+                    } else {     // Re(conj(a) b) = ar br + ai bi
+                        df_mac(vh, vl, arf.h, arf.l, brf.h, brf.l);
+                        df_mac(vh, vl, aif.h, aif.l, bif.h, bif.l);
+                    }
+                }
+                add(vh, vl, T, neg);
+            }
         }
-        // multiply by i^ny, then take Re(c * .)
-        double re = sre.value(), im = sim.value();
-        for (int r = 0; r < ny; ++r) {
-            const double tr = -im;
-            im = re;
-            re = tr;
-        }
-        total += coef[2 * t] * re - coef[2 * t + 1] * im;
     }
-    double v[1] = {total};
+    double v[1] = {(double)acc_h + (double)acc_l};
     block_sum<1>(v, red);
     if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
 }
@@ -1249,16 +1324,33 @@ struct PermSpec {
     uint8_t tile_pos[kMaxTileBits];
     uint8_t ins_pos[64];
     uint8_t src_slot[kMaxTileBits];  // for destination tile bit j: source tile bit
+    uint16_t src_lut[128];           // source tile index of destination bits 0-5 (first 64) and 6-11
 };
 
+// Shared-memory slot of tile element L: L with its low bits XORed by a fold
+// of its higher bits, so that a quarter-warp of 16-byte elements (a
+// half-warp of 8-byte ones) hits distinct bank groups both when it writes
+// consecutive elements and when it reads elements whose indices differ only
+// in high bits (the moved qubits).
+template <class S>
+__device__ __forceinline__ int perm_slot(int L) {
+    constexpr int b = sizeof(S) == 16 ? 3 : 4;
+    constexpr int m = (1 << b) - 1;
+    return L ^ (((L >> b) ^ (L >> (2 * b)) ^ (L >> (3 * b)) ^ (L >> (4 * b))) & m);
+}
+
 // In-place bit permutation, one tile at a time: every tile maps onto itself.
+// A tile is read with coalesced loads (runs of 2^w consecutive amplitudes),
+// held in shared memory and written back permuted; the source index of each
+// destination element comes from two 64-entry tables.
 template <class S>
 __global__ void __launch_bounds__(kThreads) permute_kernel(S* __restrict__ state, const __grid_constant__ PermSpec p) {
     extern __shared__ __align__(16) unsigned char smem[];
     const int Q = 1 << p.q;
     S* buf = reinterpret_cast<S*>(smem);
-    uint64_t* hoff = reinterpret_cast<uint64_t*>(buf + Q);
     const int nh = p.q - p.w;
+    uint64_t* hoff = reinterpret_cast<uint64_t*>(buf + Q);
+    uint16_t* lut = reinterpret_cast<uint16_t*>(hoff + (1 << nh));
     const uint32_t lowmask = (1u << p.w) - 1u;
     for (int j = threadIdx.x; j < (1 << nh); j += blockDim.x) {
         uint64_t o = 0;
@@ -1266,17 +1358,20 @@ __global__ void __launch_bounds__(kThreads) permute_kernel(S* __restrict__ state
             if ((j >> b) & 1) o |= 1ULL << p.tile_pos[p.w + b];
         hoff[j] = o;
     }
+    for (int j = threadIdx.x; j < 128; j += blockDim.x) lut[j] = p.src_lut[j];
     __syncthreads();
     const uint64_t ntiles = 1ULL << (p.n - p.nins);
     for (uint64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
         uint64_t base = t;
         for (int i = 0; i < p.nins; ++i) base = insert_zero(base, p.ins_pos[i]);
-        for (int L = threadIdx.x; L < Q; L += blockDim.x) buf[L] = state[base + hoff[L >> p.w] + (L & lowmask)];
+#pragma unroll 4
+        for (int L = threadIdx.x; L < Q; L += kThreads)
+            buf[perm_slot<S>(L)] = __ldcs(state + base + hoff[L >> p.w] + (L & lowmask));
         __syncthreads();
-        for (int L = threadIdx.x; L < Q; L += blockDim.x) {
-            int Ls = 0;
-            for (int j = 0; j < p.q; ++j) Ls |= ((L >> j) & 1) << p.src_slot[j];
-            state[base + hoff[L >> p.w] + (L & lowmask)] = buf[Ls];
+#pragma unroll 4
+        for (int L = threadIdx.x; L < Q; L += kThreads) {
+            const int Ls = lut[L & 63] | lut[64 + (L >> 6)];
+            __stcs(state + base + hoff[L >> p.w] + (L & lowmask), buf[perm_slot<S>(Ls)]);
         }
         __syncthreads();
     }
@@ -1552,7 +1647,9 @@ cudaError_t permute_bits(int arith, void* state, int n, int m, const uint8_t* ol
     // amplitudes (or the whole state)
     uint64_t inset = 0;
     for (int j = 0; j < m; ++j) inset |= 1ULL << oldpos[j];
-    int q = std::min(n, std::max(m, 10));
+    // 32 KiB tiles: six CTAs per SM keep enough loads in flight
+    const int qmin = arith == kArithF32 ? 12 : 11;
+    int q = std::min(n, std::max(m, qmin));
     if (q > kMaxTileBits) return cudaErrorInvalidValue;
     for (int b = 0; b < n && __builtin_popcountll(inset) < q; ++b) inset |= 1ULL << b;
     q = __builtin_popcountll(inset);
@@ -1568,10 +1665,20 @@ cudaError_t permute_bits(int arith, void* state, int n, int m, const uint8_t* ol
     for (int j = 0; j < q; ++j) slot[p.tile_pos[j]] = j;
     for (int j = 0; j < q; ++j) p.src_slot[j] = (uint8_t)j;
     for (int j = 0; j < m; ++j) p.src_slot[slot[newpos[j]]] = (uint8_t)slot[oldpos[j]];
+    for (int v = 0; v < 64; ++v) {
+        uint32_t lo = 0, hi = 0;
+        for (int j = 0; j < 6; ++j) {
+            if (((v >> j) & 1) && j < q) lo |= 1u << p.src_slot[j];
+            if (((v >> j) & 1) && j + 6 < q) hi |= 1u << p.src_slot[j + 6];
+        }
+        p.src_lut[v] = (uint16_t)lo;
+        p.src_lut[64 + v] = (uint16_t)hi;
+    }
     const size_t elem = (arith == kArithF32) ? sizeof(float2) : sizeof(double2);
-    const size_t smem = (elem << q) + sizeof(uint64_t) * (1u << (q - p.w));
+    const size_t smem = (elem << q) + sizeof(uint64_t) * (1u << (q - p.w)) + 128 * sizeof(uint16_t);
     const uint64_t ntiles = 1ULL << (n - q);
-    const unsigned g = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)device_sm_count() * 4);
+    const int per_sm = std::max(1, std::min(2048 / kThreads, (int)((227u << 10) / (smem + 1024))));
+    const unsigned g = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)device_sm_count() * per_sm);
     if (arith == kArithF32) {
         cudaFuncSetAttribute(permute_kernel<float2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         permute_kernel<float2><<<g, kThreads, smem, s>>>((float2*)state, p);

@@ -219,6 +219,40 @@ def test_expectation_known_answers(make):
         sim.get_expectation_value([([(3, "Z")], 1.0)], q)
 
 
+@pytest.mark.parametrize("prec", ["c128", "c64"])
+def test_pauli_sums_match_oracle(hqs, cuda, prec):
+    """Pauli sums with complex coefficients, Y strings, the empty string,
+    flips on low and high qubits and more terms than one chunk of the
+    expectation kernel (64), on a random state and after permuting the
+    qubits, against the oracle."""
+    from oracle.engine import OracleSimulator
+    rng = np.random.Generator(np.random.PCG64(31))
+    n = 13
+    ids = list(range(n))
+    psi = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    psi /= np.linalg.norm(psi)
+    if prec == "c64":
+        psi = psi.astype(np.complex64).astype(np.complex128)
+    op = [([], complex(0.25, -0.5))]
+    for t in range(150):
+        w = int(rng.integers(1, 5))
+        qs = sorted(int(q) for q in rng.choice(n, size=w, replace=False))
+        op.append(([(q, "XYZ"[int(rng.integers(0, 3))]) for q in qs],
+                   complex(rng.standard_normal(), rng.standard_normal())))
+    sim = hqs.SimulatorMPI(3, 20, 4, prec)
+    ref = OracleSimulator(3, 20, 4)
+    for s in (sim, ref):
+        s.allocate_qureg(ids, 0)
+        s.set_wavefunction(psi.tolist(), ids)
+    tol = 1e-11 if prec == "c128" else 1e-5
+    want = ref.get_expectation_value(op, ids)
+    assert abs(sim.get_expectation_value(op, ids) - want) < tol
+    for part in (op[:1], op[1:2], op[1:64], op[60:130]):
+        assert abs(sim.get_expectation_value(part, ids) - ref.get_expectation_value(part, ids)) < tol
+    sim.move_qubits([12, 11, 10], [0, 1, 2])
+    assert abs(sim.get_expectation_value(op, ids) - want) < tol
+
+
 def test_apply_qubit_operator_known_answers(make):
     """Commented-out reference test _simulator_mpi_test.py:454-478."""
     sim = make()

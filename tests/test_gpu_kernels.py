@@ -150,12 +150,15 @@ def test_probability_block_sums_collapse(ws, cuda, oracle_lib, arith):
 @pytest.mark.parametrize("arith", ["df", "f32"])
 def test_permute_bits_is_exact(ws, cuda, arith):
     rng = np.random.Generator(np.random.PCG64(4))
-    n = 17
-    psi = rand_state(rng, n)
     c64 = arith == "f32"
-    src = psi.astype(np.complex64).astype(np.complex128) if c64 else psi
-    for oldpos, newpos in [([0, 16], [16, 0]), ([1, 2, 3, 14, 15, 16], [14, 15, 16, 1, 2, 3]),
-                           ([0, 5, 9, 12], [5, 9, 12, 0]), (list(range(12)), list(range(11, -1, -1)))]:
+    top5 = list(range(12, 17))
+    for n, oldpos, newpos in [(17, [0, 16], [16, 0]), (17, [1, 2, 3, 14, 15, 16], [14, 15, 16, 1, 2, 3]),
+                              (17, [0, 5, 9, 12], [5, 9, 12, 0]), (17, list(range(12)), list(range(11, -1, -1))),
+                              (17, top5 + [0, 1, 2, 3, 4], [0, 1, 2, 3, 4] + top5),   # the forced permutation
+                              (20, [15, 16, 17, 18, 19, 0, 1, 2, 3, 4], [0, 1, 2, 3, 4, 15, 16, 17, 18, 19]),
+                              (7, [0, 6], [6, 0]), (5, [0, 1, 4], [4, 0, 1])]:
+        psi = rand_state(rng, n)
+        src = psi.astype(np.complex64).astype(np.complex128) if c64 else psi
         d = Dev(cuda, psi, c64=c64)
         ws.permute_bits(d.ptr, n, arith, oldpos, newpos)
         idx = np.arange(1 << n)
