@@ -162,6 +162,33 @@ __device__ __forceinline__ void digits6(double v, int Eb, float (&dg)[6]) {
     dg[5] = rnd_with(__fmul_rn(__fsub_rn(u4, dg[4]), 512.f), kMagic0);
 }
 
+// The same digits for a normalized double-float amplitude (h, l), |l| <=
+// ulp(h) / 2 (an amplitude a diagonal run has multiplied in double-float):
+// X' = (h + l) 2^(134 - Ef), Ef the largest float exponent of the group's
+// high parts, scaled in two exact steps (2^(134 - Ef) can exceed the float
+// range), then digits6's cascade from H = h 2^(134 - Ef), L = l 2^(134 - Ef).
+__device__ __forceinline__ void digits6_df(float h, float l, int Ef, float (&dg)[6]) {
+    const int k = 134 - Ef, k1 = min(k, 127), k2 = k - k1;
+    const float s1 = __uint_as_float((uint32_t)(k1 + 127) << 23), s2 = __uint_as_float((uint32_t)(k2 + 127) << 23);
+    const float H = __fmul_rn(__fmul_rn(h, s1), s2);
+    const float L = __fmul_rn(__fmul_rn(l, s1), s2);
+    const float T0 = rnd_with(H, kMagic9);
+    const float R0 = __fsub_rn(H, T0);
+    const float R27 = rnd_with(R0, kMagic27);
+    const float D = __fadd_rn(__fsub_rn(R0, R27), L);
+    const float D27 = rnd_with(D, kMagic27);
+    const float T1 = __fadd_rn(R27, D27);
+    const float T2 = __fsub_rn(D, D27);
+    dg[0] = rnd_with(T0, kMagic0);
+    dg[1] = __fmul_rn(__fsub_rn(T0, dg[0]), 512.f);
+    const float u2 = __fmul_rn(T1, 262144.f);
+    dg[2] = rnd_with(u2, kMagic0);
+    dg[3] = __fmul_rn(__fsub_rn(u2, dg[2]), 512.f);
+    const float u4 = __fmul_rn(T2, 68719476736.f);
+    dg[4] = rnd_with(u4, kMagic0);
+    dg[5] = rnd_with(__fmul_rn(__fsub_rn(u4, dg[4]), 512.f), kMagic0);
+}
+
 __device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
     __half2 h = __floats2half2_rn(lo, hi);
     return *reinterpret_cast<uint32_t*>(&h);
@@ -176,9 +203,8 @@ __device__ __forceinline__ void fast_two_sum(float a, float b, float& s, float& 
 // Output real from the six level sums: V = sum_L S_L 2^(-9 L) (level sums
 // 0-3 exact integers below 2^24, 4-5 within a few units), as a double-float
 // (h, l) by three exact fast two-sums (every partial sum lies on a grid that
-// keeps them exact), then the double h + l times 2^off assembled with
-// integer operations.
-__device__ __forceinline__ double level_sum_to_double(const float (&S)[6], int off) {
+// keeps them exact).
+__device__ __forceinline__ void level_sum_to_df(const float (&S)[6], float& h, float& l) {
     const float b1 = __fmul_rn(S[1], 1.0f / 512.f);
     const float b2 = __fmul_rn(S[2], 1.0f / 262144.f);
     const float b3 = __fmul_rn(S[3], 1.0f / 134217728.f);
@@ -189,8 +215,12 @@ __device__ __forceinline__ double level_sum_to_double(const float (&S)[6], int o
     fast_two_sum(s1, b2, s2, e2);
     fast_two_sum(s2, b3, s3, e3);
     const float t = __fadd_rn(__fadd_rn(e1, e2), __fadd_rn(e3, f));
-    float h, l;
     fast_two_sum(s3, t, h, l);
+}
+
+// The double nearest (h + l) 2^off for a normalized double-float, assembled
+// with integer operations (0 below the double range).
+__device__ __forceinline__ double df_to_double_scaled(float h, float l, int off) {
     const uint32_t hb = __float_as_uint(h);
     const int eh = (int)((hb >> 23) & 0xFFu);
     const int be = eh + 896 + off;
@@ -440,79 +470,133 @@ __global__ void __launch_bounds__(kThreadsU, 1)
         }
         __syncwarp();
     } else {
-        // ---- compute warps: digits, then outputs
+        // ---- compute warps: digits, then outputs. The runs' factor tables
+        // are built while the MMAs of the tile run: the post-run table of
+        // this tile and the pre-run table of the next (the pre-run table of
+        // the first tile before the loop). A pre-run is applied while the
+        // digits are formed (the amplitudes stay double-floats in
+        // registers), a post-run while the outputs are assembled.
         const int q4 = warp & 3, part = warp >> 2, g = q4 * 32 + lane;
         const OpDesc& tc = d.ops[u.tc_op];
         const uint32_t lane_base = (uint32_t)(q4 * 32) << 16;
+        const bool pre = u.tc_op > 0, post = u.tc_op + 1 < d.nops;
+        const int npre = pre ? 1 << __popc(u.run_mask[0]) : 0, npost = post ? 1 << __popc(u.run_mask[1]) : 0;
+        float4* tab_pre = tab;
+        float4* tab_post = tab + (1 << kUmmaRunBits);
+        const uint8_t* lut_pre = lut;
+        const uint8_t* lut_post = lut + 128;
+        auto build_pre = [&](uint64_t b) {
+            for (int i = threadIdx.x; i < npre; i += kCompute)
+                tab_pre[i] = run_entry(ewp, d, 0, u.tc_op, u.run_mask[0], (uint32_t)i, b);
+        };
+        auto build_post = [&](uint64_t b) {
+            for (int i = threadIdx.x; i < npost; i += kCompute)
+                tab_post[i] = run_entry(ewp, d, u.tc_op + 1, d.nops, u.run_mask[1], (uint32_t)i, b);
+        };
         const Walk walk(d, blockIdx.x, gridDim.x);
         uint64_t base = walk.base;
+        if (my_n > 0) build_pre(base);
         for (uint64_t it = 0; it < my_n; ++it, base = walk.after(base)) {
             const int s = (int)(it & 1);
             double2* buf = reinterpret_cast<double2*>(sm + (s ? kSmTile1 : kSmTile0));
             mbar_wait(&full[s], (uint32_t)((it >> 1) & 1), abort);
             bar_sync(1, kCompute);
             if (*abort) break;
-            const bool pre = u.tc_op > 0, post = u.tc_op + 1 < d.nops;
-            if (pre || post) {
-                for (int t = threadIdx.x; t < 2 * (1 << kUmmaRunBits); t += kCompute) {
-                    const int r = t >> kUmmaRunBits;
-                    const uint32_t i = (uint32_t)t & ((1u << kUmmaRunBits) - 1u);
-                    if ((r == 0 && !pre) || (r == 1 && !post) || i >= (1u << __popc(u.run_mask[r]))) continue;
-                    tab[t] = r == 0 ? run_entry(ewp, d, 0, u.tc_op, u.run_mask[0], i, base)
-                                    : run_entry(ewp, d, u.tc_op + 1, d.nops, u.run_mask[1], i, base);
-                }
-                bar_sync(1, kCompute);
-            }
-            if (pre) {
-                run_apply(buf, tab, lut);
-                bar_sync(1, kCompute);
-            }
             const bool act = (base & tc.ctrl_outer) == tc.ctrl_outer;
+            const uint32_t gbase = gb[g];
+            // a group whose in-tile controls are not all 1 keeps its inputs
+            // (with the runs applied)
+            const bool write = (gbase & tc.ctrl_local) == tc.ctrl_local;
             if (act) {
                 // digit planes of the tile's 128 groups; this thread: group g,
                 // inputs 8 part .. 8 part + 7
-                const uint32_t gbase = gb[g];
-                double2 x[8];
                 uint32_t mx = 0;
+                if (pre) {
+                    float4 xf[8];
 #pragma unroll
-                for (int i = 0; i < 8; ++i) {
-                    x[i] = buf[gbase | offt[part * 8 + i]];
-                    mx = max(mx, (uint32_t)__double2hiint(x[i].x) & 0x7FFFFFFFu);
-                    mx = max(mx, (uint32_t)__double2hiint(x[i].y) & 0x7FFFFFFFu);
-                }
-                mxs[threadIdx.x] = mx;
-                bar_sync(1, kCompute);
-                const int Eb = (int)(max(max(mxs[g], mxs[128 + g]), max(mxs[256 + g], mxs[384 + g])) >> 20);
-                if (part == 0) erow[g] = Eb;
-#pragma unroll
-                for (int bt = 0; bt < 2; ++bt) {
-                    uint32_t pl[6][4];
-#pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        float dr[6], di[6];
-                        digits6(x[bt * 4 + i].x, Eb, dr);
-                        digits6(x[bt * 4 + i].y, Eb, di);
-#pragma unroll
-                        for (int p = 0; p < 6; ++p) pl[p][i] = pack_h2(dr[p], di[p]);
+                    for (int i = 0; i < 8; ++i) {
+                        const uint32_t L = gbase | offt[part * 8 + i];
+                        xf[i] = ArithDF::mul(tab_pre[run_index(lut_pre, L)], ArithDFRaw::elem_load(buf[L]));
+                        if (!write) buf[L] = ArithDFRaw::elem_store(xf[i]);
+                        mx = max(mx, __float_as_uint(xf[i].x) & 0x7FFFFFFFu);
+                        mx = max(mx, __float_as_uint(xf[i].y) & 0x7FFFFFFFu);
                     }
-                    const uint32_t e0 = (uint32_t)(part * 8 + bt * 4);
+                    mxs[threadIdx.x] = mx;
+                    bar_sync(1, kCompute);
+                    const int Ef = (int)(max(max(mxs[g], mxs[128 + g]), max(mxs[256 + g], mxs[384 + g])) >> 23);
+                    if (part == 0) erow[g] = Ef == 0 ? 0 : Ef + 896;
 #pragma unroll
-                    for (int p = 0; p < 4; ++p)
-                        tmem_st4(tmem + lane_base + kTmPlanes + (uint32_t)p * 32u + e0, pl[p][0], pl[p][1], pl[p][2], pl[p][3]);
-                    const uint32_t c0 = e0 >> 2;
+                    for (int bt = 0; bt < 2; ++bt) {
+                        uint32_t pl[6][4];
 #pragma unroll
-                    for (int p = 4; p < 6; ++p) {
-                        unsigned char* row = sm + kSmPlanes + (uint32_t)(p - 4) * 16384u + (uint32_t)g * 128u;
-                        *reinterpret_cast<uint4*>(row + ((c0 ^ (g & 7)) << 4)) =
-                            make_uint4(pl[p][0], pl[p][1], pl[p][2], pl[p][3]);
+                        for (int i = 0; i < 4; ++i) {
+                            float dr[6], di[6];
+                            const float4 v = xf[bt * 4 + i];
+                            digits6_df(v.x, v.z, Ef, dr);
+                            digits6_df(v.y, v.w, Ef, di);
+#pragma unroll
+                            for (int q = 0; q < 6; ++q) pl[q][i] = pack_h2(dr[q], di[q]);
+                        }
+                        const uint32_t e0 = (uint32_t)(part * 8 + bt * 4);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            tmem_st4(tmem + lane_base + kTmPlanes + (uint32_t)q * 32u + e0, pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
+                        const uint32_t c0 = e0 >> 2;
+#pragma unroll
+                        for (int q = 4; q < 6; ++q) {
+                            unsigned char* row = sm + kSmPlanes + (uint32_t)(q - 4) * 16384u + (uint32_t)g * 128u;
+                            *reinterpret_cast<uint4*>(row + ((c0 ^ (g & 7)) << 4)) =
+                                make_uint4(pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
+                        }
+                    }
+                } else {
+                    double2 x[8];
+#pragma unroll
+                    for (int i = 0; i < 8; ++i) {
+                        x[i] = buf[gbase | offt[part * 8 + i]];
+                        mx = max(mx, (uint32_t)__double2hiint(x[i].x) & 0x7FFFFFFFu);
+                        mx = max(mx, (uint32_t)__double2hiint(x[i].y) & 0x7FFFFFFFu);
+                    }
+                    mxs[threadIdx.x] = mx;
+                    bar_sync(1, kCompute);
+                    const int Eb = (int)(max(max(mxs[g], mxs[128 + g]), max(mxs[256 + g], mxs[384 + g])) >> 20);
+                    if (part == 0) erow[g] = Eb;
+#pragma unroll
+                    for (int bt = 0; bt < 2; ++bt) {
+                        uint32_t pl[6][4];
+#pragma unroll
+                        for (int i = 0; i < 4; ++i) {
+                            float dr[6], di[6];
+                            digits6(x[bt * 4 + i].x, Eb, dr);
+                            digits6(x[bt * 4 + i].y, Eb, di);
+#pragma unroll
+                            for (int q = 0; q < 6; ++q) pl[q][i] = pack_h2(dr[q], di[q]);
+                        }
+                        const uint32_t e0 = (uint32_t)(part * 8 + bt * 4);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q)
+                            tmem_st4(tmem + lane_base + kTmPlanes + (uint32_t)q * 32u + e0, pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
+                        const uint32_t c0 = e0 >> 2;
+#pragma unroll
+                        for (int q = 4; q < 6; ++q) {
+                            unsigned char* row = sm + kSmPlanes + (uint32_t)(q - 4) * 16384u + (uint32_t)g * 128u;
+                            *reinterpret_cast<uint4*>(row + ((c0 ^ (g & 7)) << 4)) =
+                                make_uint4(pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
+                        }
                     }
                 }
                 tmem_st_wait();
                 fence_proxy_async();
+            } else if (pre) {
+                // the dense gate leaves this tile alone: the runs apply as they are
+                run_apply(buf, tab_pre, lut_pre);
             }
             fence_before_sync();
             bar_sync(1, kCompute);
             if (threadIdx.x == 0) mbar_arrive(pbar);
+            // while the MMAs run: this tile's post-run table, the next tile's pre-run table
+            if (post) build_post(base);
+            if (pre && it + 1 < my_n) build_pre(walk.after(base));
             mbar_wait(mbar, (uint32_t)(it & 1), abort);
             bar_sync(1, kCompute);
             if (*abort) break;
@@ -520,10 +604,8 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             if (act) {
                 // outputs: group g, output reals 16 part .. 16 part + 15. The
                 // tensor-memory loads are warp-collective: every thread takes
-                // part; a group whose controls are not all 1 keeps its inputs.
-                const bool write = (gb[g] & tc.ctrl_local) == tc.ctrl_local;
+                // part, also for a group that keeps its inputs.
                 const int Eb = erow[g];
-                const uint32_t gbase = gb[g];
 #pragma unroll
                 for (int ch = 0; ch < 2; ++ch) {
                     const uint32_t n0 = (uint32_t)(part * 16 + ch * 8);
@@ -533,26 +615,40 @@ __global__ void __launch_bounds__(kThreadsU, 1)
                     tmem_ld_wait();
 #pragma unroll
                     for (int a = 0; a < 4; ++a) {
-                        double out[2];
+                        const uint32_t L = gbase | offt[(n0 >> 1) + a];
+                        if (!write) {  // the pre-run was stored with the digits
+                            if (post)
+                                buf[L] = ArithDFRaw::elem_store(
+                                    ArithDF::mul(tab_post[run_index(lut_post, L)], ArithDFRaw::elem_load(buf[L])));
+                            continue;
+                        }
+                        float h[2], l[2];
 #pragma unroll
                         for (int p = 0; p < 2; ++p) {
                             const int c = a * 2 + p;
                             const float S[6] = {__uint_as_float(r[0][c]), __uint_as_float(r[1][c]),
                                                 __uint_as_float(r[2][c]), __uint_as_float(r[3][c]),
                                                 __uint_as_float(r[4][c]), __uint_as_float(r[5][c])};
-                            out[p] = Eb == 0 ? 0.0 : level_sum_to_double(S, Eb + ecol[n0 + c] - 2059);
+                            level_sum_to_df(S, h[p], l[p]);
                         }
-                        if (write) buf[gbase | offt[(n0 >> 1) + a]] = make_double2(out[0], out[1]);
+                        if (post) {
+                            const float4 v = ArithDF::mul(tab_post[run_index(lut_post, L)], make_float4(h[0], h[1], l[0], l[1]));
+                            h[0] = v.x;
+                            h[1] = v.y;
+                            l[0] = v.z;
+                            l[1] = v.w;
+                        }
+                        const int c0 = a * 2;
+                        buf[L] = Eb == 0 ? make_double2(0.0, 0.0)
+                                         : make_double2(df_to_double_scaled(h[0], l[0], Eb + ecol[n0 + c0] - 2059),
+                                                        df_to_double_scaled(h[1], l[1], Eb + ecol[n0 + c0 + 1] - 2059));
                     }
                 }
-            }
-            fence_before_sync();
-            bar_sync(1, kCompute);
-            if (post) {
-                run_apply(buf, tab + (1 << kUmmaRunBits), lut + 128);
-                bar_sync(1, kCompute);
+            } else if (post) {
+                run_apply(buf, tab_post, lut_post);
             }
             fence_proxy_async();
+            fence_before_sync();
             bar_sync(1, kCompute);
             if (threadIdx.x == 0) mbar_arrive(&tdone[s]);
         }

@@ -101,6 +101,27 @@ def test_umma_diagonal_runs_around_the_dense_gate(ws, cuda, oracle_lib):
     assert plan[0]["umma"] and plan[0]["nops"] == len(gates)
 
 
+@pytest.mark.parametrize("ctrl", [1 << 2, 1 << 19, (1 << 0) | (1 << 17)])
+def test_umma_runs_around_a_controlled_dense_gate(ws, cuda, oracle_lib, ctrl):
+    """Runs before and after a dense gate whose controls sit inside the tile
+    (groups that keep their inputs still take both runs), outside it (tiles
+    the gate leaves alone) or both; the runs carry their own controls."""
+    rng = np.random.Generator(np.random.PCG64(400 + ctrl % 97))
+    n = 20
+    gates = [diag(rng, [0, 2, 19]), scalar(rng), diag(rng, [3, 16], ctrl=1 << 9),
+             dense(rng, [1, 6, 11, 14, 18], ctrl=ctrl),
+             diag(rng, [2, 4, 7, 17]), diag(rng, [19, 0]), scalar(rng)]
+    plan = run_case(ws, cuda, oracle_lib, n, gates, rng)
+    assert plan[0]["umma"] and plan[0]["nops"] == len(gates)
+
+
+def test_umma_runs_only_before_or_only_after(ws, cuda, oracle_lib):
+    rng = np.random.Generator(np.random.PCG64(402))
+    n = 18
+    run_case(ws, cuda, oracle_lib, n, [diag(rng, [0, 9, 17]), dense(rng, [2, 5, 8, 12, 15])], rng)
+    run_case(ws, cuda, oracle_lib, n, [dense(rng, [2, 5, 8, 12, 15]), diag(rng, [1, 9, 16]), scalar(rng)], rng)
+
+
 def test_umma_sequences_of_passes_on_a_larger_state(ws, cuda, oracle_lib):
     """Many tiles per CTA (the two-buffer copy pipeline), several passes in
     a row, gates whose targets move between low and high positions."""

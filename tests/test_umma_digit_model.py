@@ -1,5 +1,6 @@
 """Exact CPU model of the digit arithmetic of the tensor-memory pass
-(umma_pass.cu: digits6, level_sum_to_double; workspace.cpp: gate_digits9).
+(umma_pass.cu: digits6, digits6_df, level_sum_to_df + df_to_double_scaled;
+workspace.cpp: gate_digits9).
 
 State reals: six balanced base-2^9 digits of X' = v 2^(1030 - E_row), computed
 with the kernel's FP32 operations (numpy float32, round to nearest even).
@@ -96,8 +97,8 @@ def fast_two_sum(a, b):
 
 
 def level_sum_to_double(S, off):
-    """umma_pass.cu level_sum_to_double; S: six level sums as float32 (the
-    accumulators), off = E_row + E_col - 2059."""
+    """umma_pass.cu level_sum_to_df then df_to_double_scaled; S: six level
+    sums as float32 (the accumulators), off = E_row + E_col - 2059."""
     S = [F(x) for x in S]
     b1 = F(S[1] * F(1.0 / 512))
     b2 = F(S[2] * F(1.0 / 262144))
@@ -210,3 +211,63 @@ def test_umma_digits_aligned_worst_cases():
     xt = np.array([(base + 2.0 ** -30 * (k + 1)) * 2.0 ** -40 * (-1) ** k for k in range(64)])
     check_row(xt, b, range(0, 64, 13), stats)
     assert stats["out"] < 2.0 ** -45, stats
+
+
+def digits6_df(h, l, ebf_row):
+    """umma_pass.cu digits6_df: the six digits of (h + l) 2^(134 - E_row)
+    for a normalized double-float (|l| <= ulp(h) / 2), E_row the largest
+    float exponent of the group's high parts; the scaling in two exact
+    steps, then digits6's cascade."""
+    k = 134 - ebf_row
+    k1 = min(k, 127)
+    k2 = k - k1
+    s1, s2 = _f32_from_bits((k1 + 127) << 23), _f32_from_bits((k2 + 127) << 23)
+    H = F(F(F(h) * s1) * s2)
+    L = F(F(F(l) * s1) * s2)
+    T0 = rnd_with(H, M9)
+    R0 = F(H - T0)
+    R27 = rnd_with(R0, M27)
+    D = F(F(R0 - R27) + L)
+    D27 = rnd_with(D, M27)
+    T1 = F(R27 + D27)
+    T2 = F(D - D27)
+    d0 = rnd_with(T0, M0)
+    d1 = F(F(T0 - d0) * F(512))
+    u2 = F(T1 * F(262144))
+    d2 = rnd_with(u2, M0)
+    d3 = F(F(u2 - d2) * F(512))
+    u4 = F(T2 * F(68719476736.0))
+    d4 = rnd_with(u4, M0)
+    d5 = rnd_with(F(F(u4 - d4) * F(512)), M0)
+    out = [d0, d1, d2, d3, d4, d5]
+    assert all(float(x) == int(x) for x in out)
+    return [int(x) for x in out]
+
+
+def test_umma_digits_from_double_float():
+    """Digits of double-float amplitudes (a diagonal run applied before the
+    dense gate, kept as double-floats): bounds |d| <= 256 (d_2 <= 260) and
+    the value to 2^-46 of the group's scale, over groups with a wide
+    exponent range, exact zeros, ties and groups of tiny amplitudes (the
+    two-step scaling)."""
+    rng = np.random.default_rng(17)
+    worst = 0.0
+    for trial in range(40):
+        scale = 2.0 ** -int(rng.integers(0, 140)) if trial % 5 == 4 else 2.0 ** -int(rng.integers(0, 30))
+        x = rng.standard_normal(64) * np.exp(rng.uniform(-12, 0, 64)) * scale
+        x[rng.random(64) < 0.1] = 0.0
+        hs = [F(v) for v in x]
+        ls = [F(v - float(hv)) for v, hv in zip(x, hs)]
+        if trial % 7 == 3:  # ties of the 2^-9 grid in H
+            hs[0] = F(2.0 ** 7 * (1 + 2.0 ** -17) * scale)
+            ls[0] = F(2.0 ** -30 * scale)
+        ebf = max((_f32_bits(v) >> 23) & 0xFF for v in hs)
+        if ebf == 0:
+            continue
+        for hv, lv in zip(hs, ls):
+            d = digits6_df(hv, lv, ebf)
+            assert max(abs(d[i]) for i in (0, 1, 3, 4, 5)) <= 256 and abs(d[2]) <= 260, d
+            val = sum(Fraction(di) * Fraction(2) ** (-9 * i) for i, di in enumerate(d)) * Fraction(2) ** (ebf - 134)
+            err = abs(val - (Fraction(float(hv)) + Fraction(float(lv))))
+            worst = max(worst, float(err / Fraction(2) ** (ebf - 126)))
+    assert worst < 2.0 ** -46, worst
