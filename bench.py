@@ -706,6 +706,10 @@ def run_ours(args, dist):
     pt = sim.pass_timing()
     sim.enable_pass_timing(False)
     clk = clocks.stop()
+    if args.pass_log:
+        for k, (kname, nops, byts, lms, copies, tmask) in enumerate(pt["log"]):
+            log("launch %3d %-17s ops %2d  %7.2f ms  copies %2d  targets %s" % (
+                k, kname, nops, lms, copies, [b for b in range(64) if (tmask >> b) & 1]))
     s1 = sim.stats()
     ms = dist.max(ms)
     dist.barrier()
@@ -724,7 +728,7 @@ def run_ours(args, dist):
     nl = max(pt["launches"], 1)
     algo = args.steps * pass_ref_bytes
     kinds = {}
-    for kname, nops, byts, lms in pt["log"]:
+    for kname, nops, byts, lms, _, _ in pt["log"]:
         k = kinds.setdefault(kname, {"launches": 0, "bytes": 0, "ms": 0.0, "ops": 0})
         k["launches"] += 1
         k["bytes"] += byts
@@ -849,6 +853,7 @@ def main():
     ap.add_argument("--no-precision", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the comparisons with the oracle")
     ap.add_argument("--tour", action="store_true", help="launch every state-streaming kernel once (profiling)")
+    ap.add_argument("--pass-log", action="store_true", help="print every timed pass launch")
     ap.add_argument("--capacity", action="store_true", help="also run the 33q c128 / 34q c64 capacity states")
     ap.add_argument("--table", action="store_true", help="also time the reference-against-GPU table rows")
     args = ap.parse_args()

@@ -388,6 +388,9 @@ int hqs_sim_pass_log(hqs_sim* sim, hqs_pass_record* out, size_t cap, size_t* cou
             const auto& r = sim->pass_log[i];
             out[i].kernel = r.kind;
             out[i].nops = r.nops;
+            out[i].copies = r.copies;
+            out[i].pad = 0;
+            out[i].target_mask = r.target_mask;
             out[i].bytes = r.bytes;
             out[i].ms = r.ms;
         }

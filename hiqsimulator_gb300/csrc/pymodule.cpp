@@ -308,7 +308,7 @@ public:
         py::list log;
         for (const auto& r : rec)
             log.append(py::make_tuple(r.kernel == HQS_KERNEL_UMMA ? "umma_pass_kernel" : "pass_kernel", r.nops,
-                                      r.bytes, r.ms));
+                                      r.bytes, r.ms, r.copies, r.target_mask));
         d["log"] = log;
         return d;
     }

@@ -838,7 +838,11 @@ uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<G
         for (size_t li = 0; li < L.size(); ++li) {
             const auto& l = L[li];
             const size_t lend = li + 1 < L.size() ? L[li + 1].first : ops.size();
-            TimedLaunch tl{nullptr, nullptr, l.bytes, l.umma ? 1 : 0, (int)(lend - l.first)};
+            uint64_t tmask = 0;
+            if (l.umma)
+                for (int j = 0; j < 5; ++j) tmask |= 1ULL << l.udesc.d.tile_pos[l.udesc.tslot[j]];
+            TimedLaunch tl{nullptr, nullptr, l.bytes, l.umma ? 1 : 0, (int)(lend - l.first),
+                           l.umma ? 1 << l.udesc.nextra : 0, tmask};
             if (timing_) {
                 tl.a = take_event();
                 tl.b = take_event();
@@ -878,7 +882,7 @@ uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<G
     for (size_t pi = 0; pi < plans.size(); ++pi) {
         const PassPlan& p = plans[pi];
         const size_t pend = pi + 1 < plans.size() ? first[pi + 1] : ops.size();
-        TimedLaunch tl{nullptr, nullptr, p.bytes, 0, (int)(pend - first[pi])};
+        TimedLaunch tl{nullptr, nullptr, p.bytes, 0, (int)(pend - first[pi]), 0, 0};
         if (timing_) {
             tl.a = take_event();
             tl.b = take_event();
@@ -916,7 +920,7 @@ Workspace::PassTiming Workspace::collect_timing() {
         t.ms += ms;
         t.bytes += tl.bytes;
         ++t.launches;
-        t.log.push_back({tl.kind, tl.nops, tl.bytes, (double)ms});
+        t.log.push_back({tl.kind, tl.nops, tl.copies, tl.target_mask, tl.bytes, (double)ms});
         event_pool_.push_back(tl.a);
         event_pool_.push_back(tl.b);
     }

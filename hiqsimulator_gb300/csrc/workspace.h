@@ -73,6 +73,8 @@ public:
     struct LaunchRecord {
         int kind = 0;  // 0: pass kernel, 1: tensor-memory pass
         int nops = 0;  // gate ops the launch applies
+        int copies = 0;  // tensor-memory pass: TMA copies per tile
+        uint64_t target_mask = 0;  // tensor-memory pass: the dense gate's five (padded) target positions
         uint64_t bytes = 0;
         double ms = 0.0;
     };
@@ -105,7 +107,8 @@ private:
     struct TimedLaunch {
         cudaEvent_t a, b;
         uint64_t bytes;
-        int kind, nops;
+        int kind, nops, copies;
+        uint64_t target_mask;
     };
     std::vector<TimedLaunch> timed_;
     std::vector<cudaEvent_t> event_pool_;

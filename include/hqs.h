@@ -174,13 +174,17 @@ int hqs_sim_set_pass_timing(hqs_sim* sim, int on);
 int hqs_sim_pass_timing(hqs_sim* sim, uint64_t* launches, uint64_t* bytes, double* ms);
 /* The launches behind the last hqs_sim_pass_timing call, in launch order:
  * kernel (HQS_KERNEL_PASS: the tiled pass kernel; HQS_KERNEL_UMMA: the
- * tensor-memory pass), gate ops applied, algorithmic HBM bytes and device
+ * tensor-memory pass), gate ops applied, TMA copies per tile and target
+ * positions of a tensor-memory pass, algorithmic HBM bytes and device
  * milliseconds. Up to cap records are written; *count receives the total. */
 #define HQS_KERNEL_PASS 0
 #define HQS_KERNEL_UMMA 1
 typedef struct {
     int32_t kernel;
     int32_t nops;
+    int32_t copies;        /* HQS_KERNEL_UMMA: TMA copies per tile (else 0) */
+    int32_t pad;
+    uint64_t target_mask;  /* HQS_KERNEL_UMMA: the dense gate's five (padded) target positions */
     uint64_t bytes;
     double ms;
 } hqs_pass_record;
