@@ -108,7 +108,8 @@ class LaunchInfo(ctypes.Structure):
                 ("tc_op", ctypes.c_uint32), ("tile_mask", ctypes.c_uint64), ("target_mask", ctypes.c_uint64),
                 ("fixed_mask", ctypes.c_uint64), ("rank", ctypes.c_uint32), ("nextra", ctypes.c_uint32),
                 ("box_bytes", ctypes.c_uint32), ("dim_kind", ctypes.c_int32 * 5), ("dim_pos", ctypes.c_int32 * 5),
-                ("dim_bits", ctypes.c_int32 * 5), ("pool_bytes", ctypes.c_uint64), ("sweep_bytes", ctypes.c_uint64)]
+                ("dim_bits", ctypes.c_int32 * 5), ("dim_box", ctypes.c_int32 * 5), ("pool_bytes", ctypes.c_uint64),
+                ("sweep_bytes", ctypes.c_uint64)]
 
 
 def plan_launches(n, arith, gates, max_tile_bits=0, max_ops=0):

@@ -689,6 +689,7 @@ int hqs_plan_launches(int n, int arith, int nops, const int* k, const int* pos, 
                     o.dim_kind[j] = j < u.rank ? u.dim_kind[j] : -1;
                     o.dim_pos[j] = u.dim_pos[j];
                     o.dim_bits[j] = u.dim_bits[j];
+                    o.dim_box[j] = u.dim_box[j];
                 }
             }
         }

@@ -95,10 +95,12 @@ struct UmmaDesc {
     uint8_t rank;          // tensor-map rank (1..5)
     uint8_t nextra;        // tile bits above the box (one copy per combination)
     uint8_t pad0;
-    int8_t dim_kind[5];    // 0: inside the box (coordinate 0); 1: gap (from the tile base);
-                           // 2: rest (tile base plus the copy's extra bits)
+    int8_t dim_kind[5];    // 1: a run of tile positions (the box) and the gap above it (coordinate
+                           // from the tile base); 2: the same, last, with the extra tile bits above
+                           // its run (coordinate from the tile base plus the copy's extra bits)
     int8_t dim_pos[5];     // first state position of each dimension
     int8_t dim_bits[5];    // state positions each dimension spans
+    int8_t dim_box[5];     // of them, the run of tile positions at the bottom (inside the box)
     int8_t extra_pos[kMaxTileBits];  // state positions of the extra tile bits, ascending
     uint32_t run_mask[2];  // tile slots the element-wise run before (0) / after (1) the dense gate
                            // depends on (targets and controls inside the tile), at most kUmmaRunBits

@@ -102,22 +102,22 @@ struct Walk {
     __device__ uint64_t after(uint64_t b) const { return ((((b & spread) | ~spread) + step) & spread) | fixed; }
 };
 
-// TMA box coordinates of copy c of the tile with base index b
+// TMA box coordinates of copy c of the tile with base index b: the tile
+// base's bits of each dimension (zero over the box run), in the last
+// dimension of a plan with extra tile bits also the copy's extra bits;
+// dimension 0 counts doubles (two per amplitude)
 __device__ __forceinline__ void tile_coords(const UmmaDesc& u, uint64_t b, uint32_t c, int32_t (&co)[5]) {
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
-        int32_t v = 0;
+        uint64_t v = 0;
         if (i < u.rank) {
-            if (u.dim_kind[i] == 1) {
-                v = (int32_t)((b >> u.dim_pos[i]) & ((1ULL << u.dim_bits[i]) - 1ULL));
-            } else if (u.dim_kind[i] == 2) {
-                uint64_t r = b >> u.dim_pos[i];
+            v = (b >> u.dim_pos[i]) & ((1ULL << u.dim_bits[i]) - 1ULL);
+            if (u.dim_kind[i] == 2)
                 for (int k = 0; k < u.nextra; ++k)
-                    if ((c >> k) & 1u) r |= 1ULL << (u.extra_pos[k] - u.dim_pos[i]);
-                v = (int32_t)r;
-            }
+                    if ((c >> k) & 1u) v |= 1ULL << (u.extra_pos[k] - u.dim_pos[i]);
+            if (i == 0) v <<= 1;
         }
-        co[i] = v;
+        co[i] = (int32_t)v;
     }
 }
 
@@ -704,7 +704,7 @@ cudaError_t launch_umma_pass(void* state, const void* mats, const UmmaDesc& u, c
     cuuint32_t box[5], es[5];
     for (int i = 0; i < u.rank; ++i) {
         gdim[i] = (i == 0 ? 2ULL : 1ULL) << u.dim_bits[i];
-        box[i] = u.dim_kind[i] == 0 ? (cuuint32_t)gdim[i] : 1u;
+        box[i] = (i == 0 ? 2u : 1u) << u.dim_box[i];
         es[i] = 1;
         if (i > 0) gstr[i - 1] = 16ULL << u.dim_pos[i];
     }

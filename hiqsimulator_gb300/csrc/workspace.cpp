@@ -667,52 +667,45 @@ static int build_umma(int n, const GateOp* ops, size_t i0, size_t tc, size_t i1,
     u.ew_bytes = (uint32_t)ewb;
     u.gate_off = (uint32_t)((ewb + 1023) & ~(size_t)1023);
 
-    // TMA plan: the state as doubles, dimensions spanning consecutive
-    // positions: runs of tile positions (inside the box), gaps between them
-    // (coordinate from the tile base); when more than five dimensions would
-    // be needed, the last one spans everything above and the tile positions
-    // in it are fetched as separate copies.
-    struct Range {
-        int pos, bits;
-        bool tile;
+    // TMA plan: the state as doubles; every dimension spans a run of tile
+    // positions (inside the box, at most 256 elements: 7 positions for the
+    // first dimension with its re/im pair, 8 for the others) and the gap of
+    // non-tile positions above it (its coordinate comes from the tile base).
+    // With more than five runs the fifth dimension spans everything from its
+    // run up, and the tile positions above that run are fetched as separate
+    // copies.
+    struct Dim {
+        int pos, box, bits;
     };
-    std::vector<Range> ranges;
+    std::vector<Dim> dims;
     for (int b = 0; b < n;) {
-        const bool t = ((tile >> b) & 1ULL) != 0;
         int e = b;
-        while (e < n && (((tile >> e) & 1ULL) != 0) == t) ++e;
-        int start = b;
-        // a box dimension spans at most 256 elements: 7 positions for the
-        // first (with the re/im pair), 8 for the others
-        while (start < e) {
-            const int cap = t ? (start == 0 ? 7 : 8) : 64;
-            const int len = std::min(cap, e - start);
-            ranges.push_back({start, len, t});
-            start += len;
+        while (e < n && ((tile >> e) & 1ULL)) ++e;
+        while (e - b > (b == 0 ? 7 : 8)) {  // a run longer than a box dimension takes two
+            const int cap = b == 0 ? 7 : 8;
+            dims.push_back({b, cap, cap});
+            b += cap;
         }
-        b = e;
+        int g = e;
+        while (g < n && !((tile >> g) & 1ULL)) ++g;
+        dims.push_back({b, e - b, g - b});
+        b = g;
     }
     int rank = 0, tbits = 0;
-    for (size_t r = 0; r < ranges.size(); ++r) {
-        const bool last = r + 1 == ranges.size();
-        if (rank < 4 || last) {
-            u.dim_kind[rank] = ranges[r].tile ? 0 : 1;
-            u.dim_pos[rank] = (int8_t)ranges[r].pos;
-            u.dim_bits[rank] = (int8_t)ranges[r].bits;
-            if (ranges[r].tile) tbits += ranges[r].bits;
-            ++rank;
-            continue;
-        }
-        // rest: everything from this range up
-        u.dim_kind[rank] = 2;
-        u.dim_pos[rank] = (int8_t)ranges[r].pos;
-        u.dim_bits[rank] = (int8_t)(n - ranges[r].pos);
+    for (size_t r = 0; r < dims.size() && rank < 5; ++r) {
+        const bool rest = rank == 4 && r + 1 < dims.size();
+        u.dim_kind[rank] = rest ? 2 : 1;
+        u.dim_pos[rank] = (int8_t)dims[r].pos;
+        u.dim_box[rank] = (int8_t)dims[r].box;
+        u.dim_bits[rank] = (int8_t)(rest ? n - dims[r].pos : dims[r].bits);
+        tbits += dims[r].box;
         ++rank;
-        int ne = 0;
-        for (int b = ranges[r].pos; b < n; ++b)
-            if ((tile >> b) & 1ULL) u.extra_pos[ne++] = (int8_t)b;
-        u.nextra = (uint8_t)ne;
-        break;
+        if (rest) {
+            int ne = 0;
+            for (int b = dims[r].pos + dims[r].box; b < n; ++b)
+                if ((tile >> b) & 1ULL) u.extra_pos[ne++] = (int8_t)b;
+            u.nextra = (uint8_t)ne;
+        }
     }
     u.rank = (uint8_t)rank;
     if (tbits + u.nextra != kUmmaTileBits) return kUmmaNo;

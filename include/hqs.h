@@ -308,7 +308,9 @@ typedef struct {
     uint64_t fixed_mask;       /* control positions outside the tile every gate shares */
     uint32_t rank, nextra;     /* tensor-memory pass: TMA tensor rank, tile bits fetched as separate copies */
     uint32_t box_bytes;        /* tensor-memory pass: bytes of one TMA box */
-    int32_t dim_kind[5], dim_pos[5], dim_bits[5];  /* TMA dimensions: 0 box, 1 gap, 2 rest; first position; positions */
+    int32_t dim_kind[5], dim_pos[5], dim_bits[5];  /* TMA dimensions: 1 box run + gap above it, 2 the same
+                                                      with extra tile bits (last); first position; positions */
+    int32_t dim_box[5];        /* of each dimension's positions, the box run at its bottom */
     uint64_t pool_bytes, sweep_bytes;
 } hqs_launch_info;
 int hqs_plan_launches(int n, int arith, int nops, const int* k, const int* pos, const uint64_t* ctrl, const int* diag,

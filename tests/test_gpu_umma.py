@@ -65,6 +65,8 @@ TARGETS = [
     (22, [2, 9, 12, 16, 21]),
     (24, [1, 6, 13, 18, 23]),       # includes outputs just below a power of two
     (24, [0, 1, 2, 3, 4]),
+    (24, [8, 10, 12, 17, 21]),      # six runs of tile positions: two copies per tile
+    (20, [7, 9, 11, 13, 15]),       # runs next to the low run
 ]
 
 

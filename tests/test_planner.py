@@ -126,25 +126,26 @@ def _check_umma_launch(n, L, gates):
     for p in g[1]:
         assert (tmask >> p) & 1
     assert tmask & g[2] == 0  # controls are never targets of the widened gate
-    # TMA dimensions cover positions 0..n-1 in order; box dimensions are runs
-    # of tile positions (at most 256 elements), gaps hold no tile position,
-    # the rest dimension (if any) is last and its tile positions are copies
+    # TMA dimensions cover positions 0..n-1 in order; each starts with a run
+    # of tile positions (the box, at most 256 elements) and holds no other
+    # tile position above it, except the last dimension of a plan with extra
+    # tile bits, whose tile positions above its run are the copies
     pos, tbits = 0, 0
     rank = L["rank"]
     assert 1 <= rank <= 5
     for i in range(rank):
-        kind, p, b = L["dim_kind"][i], L["dim_pos"][i], L["dim_bits"][i]
-        assert p == pos and b >= 1
-        span = ((1 << b) - 1) << p
-        if kind == 0:
-            assert span & tile == span
-            assert b <= (7 if i == 0 else 8)
-            tbits += b
-        elif kind == 1:
-            assert span & tile == 0
+        kind, p, b, bx = L["dim_kind"][i], L["dim_pos"][i], L["dim_bits"][i], L["dim_box"][i]
+        assert p == pos and b >= 1 and 1 <= bx <= b
+        run = ((1 << bx) - 1) << p
+        above = ((1 << (b - bx)) - 1) << (p + bx)
+        assert run & tile == run
+        assert bx <= (7 if i == 0 else 8)
+        tbits += bx
+        if kind == 1:
+            assert above & tile == 0
         else:
             assert kind == 2 and i == rank - 1
-            assert bin(span & tile).count("1") == L["nextra"]
+            assert bin(above & tile).count("1") == L["nextra"]
         pos += b
     assert pos == n
     assert tbits + L["nextra"] == 12
