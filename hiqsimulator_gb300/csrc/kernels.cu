@@ -607,6 +607,12 @@ __device__ __forceinline__ void apply_tf32(const float2* __restrict__ src, float
     for (int task = warp; task < MT * NCH; task += nwarps) {
         const int mt = task / NCH, nc = task % NCH;
         const uint32_t Lb0 = group_base(mt * 16 + gid), Lb1 = group_base(mt * 16 + gid + 8);
+        // The tensor cores round their FP32 accumulation toward zero, so a
+        // long accumulation chain at full scale shrinks every output (the
+        // norm drifts down gate after gate). Each k-step's three products
+        // go into a zeroed accumulator (one truncation, at the scale of
+        // that k-step's partial sum, whose sign varies) and are added to the
+        // running sum with a round-to-nearest FADD.
         float acc[NTW][4];
 #pragma unroll
         for (int j = 0; j < NTW; ++j)
@@ -629,9 +635,12 @@ __device__ __forceinline__ void apply_tf32(const float2* __restrict__ src, float
 #pragma unroll
             for (int j = 0; j < NTW; ++j) {
                 const float4 b = frag[(ks * NT + nc * NTW + j) * 32 + lane];
-                mma_tf32(acc[j], al, __float_as_uint(b.x), __float_as_uint(b.y));
-                mma_tf32(acc[j], ah, __float_as_uint(b.z), __float_as_uint(b.w));
-                mma_tf32(acc[j], ah, __float_as_uint(b.x), __float_as_uint(b.y));
+                float t[4] = {0.f, 0.f, 0.f, 0.f};
+                mma_tf32(t, al, __float_as_uint(b.x), __float_as_uint(b.y));
+                mma_tf32(t, ah, __float_as_uint(b.z), __float_as_uint(b.w));
+                mma_tf32(t, ah, __float_as_uint(b.x), __float_as_uint(b.y));
+#pragma unroll
+                for (int e = 0; e < 4; ++e) acc[j][e] = __fadd_rn(acc[j][e], t[e]);
             }
         }
         // columns 2 tig, 2 tig + 1 of n-tile nt: output nt * 4 + tig
