@@ -1,9 +1,11 @@
-// Tensor-memory fused pass for complex128 states on sm_103a: one dense
-// k-qubit gate (k <= 5, widened to five targets with identity factors) on the
-// tcgen05 tensor cores, plus the runs of diagonal and scalar gates before and
-// after it, in one sweep over the state. Replaces, for its pass, the
-// reference's kernelK sweep (src/simulator-mpi/kernels/nointrin/kernel5.hpp:
-// 1134-1193) and the diagonal sweeps (kernels_diag.hpp:20-81).
+// Tensor-memory fused pass on sm_103a: one dense k-qubit gate (k <= 5,
+// widened to five targets with identity factors) on the tcgen05 tensor cores,
+// plus the runs of diagonal and scalar gates before and after it, in one
+// sweep over the state. Replaces, for its pass, the reference's kernelK sweep
+// (src/simulator-mpi/kernels/nointrin/kernel5.hpp:1134-1193) and the diagonal
+// sweeps (kernels_diag.hpp:20-81). Two instances: complex128 states (below)
+// and complex64 states (three digits per real, levels 0-3, all exact; see
+// the complex64 section).
 //
 // Tile: 4096 amplitudes = 128 index groups x 32 inputs (the five target bits).
 // Per tile the gate is the real GEMM Y[128 x 64] = X[128 x 64] B[64 x 64]
@@ -54,28 +56,53 @@ constexpr int kCompute = 512;  // warps 0..15
 constexpr int kTmaWarp = 16, kMmaWarp = 17;
 constexpr int kThreadsU = 576;
 
-// shared memory, relative to a 1024-byte aligned base
-constexpr uint32_t kSmGate = 0;             // 6 gate digit planes, 64 rows x 128 B each
-constexpr uint32_t kSmPlanes = 49152;       // state digit planes 4 and 5, 128 rows x 128 B each
-constexpr uint32_t kSmTile0 = 81920;        // tile buffers, 4096 x double2
-constexpr uint32_t kSmTile1 = 147456;
-constexpr uint32_t kSmEcol = 212992;        // int[64]: gate column exponents
-constexpr uint32_t kSmErow = kSmEcol + 256; // int[128]: group exponents of the current tile
-constexpr uint32_t kSmMx = kSmErow + 512;   // uint32[512]: quarter-group maxima
-constexpr uint32_t kSmGb = kSmMx + 2048;    // uint16[128]: tile index of each group's input 0
-constexpr uint32_t kSmOff = kSmGb + 256;    // uint16[32]: tile offset of each input
-constexpr uint32_t kSmBar = kSmOff + 64;    // 6 mbarriers
-constexpr uint32_t kSmMisc = kSmBar + 64;   // tensor-memory base, abort flag
-constexpr uint32_t kSmLut = kSmMisc + 64;   // uint8[2][2][64]: factor-table index of tile slots 0-5 / 6-11
-constexpr uint32_t kSmTab = kSmLut + 256;   // float4[2][256]: the runs' factor tables of the current tile
-constexpr uint32_t kSmEw = kSmTab + 2 * (1u << kUmmaRunBits) * 16;  // element-wise matrices (float4)
-constexpr uint32_t kSmBytes = kSmEw + kUmmaEwMaxBytes + 1024;  // + alignment slack
+// Shared memory (relative to a 1024-byte aligned base) and tensor memory of
+// the two instances.
+template <bool C64>
+struct Lay;
+template <>
+struct Lay<false> {  // complex128
+    static constexpr int kDigits = 6;
+    static constexpr uint32_t kGate = 0;         // 6 gate digit planes, 64 rows x 128 B each
+    static constexpr uint32_t kGateBytes = kUmmaGatePlaneBytes;
+    static constexpr uint32_t kPlanes = 49152;   // state digit planes 4 and 5, 128 rows x 128 B each
+    static constexpr uint32_t kTile0 = 81920;    // tile buffers, 4096 x double2
+    static constexpr uint32_t kTile1 = 147456;
+    static constexpr uint32_t kTileBytes = 4096 * 16;
+    static constexpr uint32_t kEcol = 212992;
+    static constexpr uint32_t kTmPlanes = 384;   // tensor-memory columns: six level regions of 64, then planes 0-3
+    static constexpr uint32_t kTabEntry = 16;    // factor-table entry: double-float complex
+};
+template <>
+struct Lay<true> {  // complex64
+    static constexpr int kDigits = 3;
+    static constexpr uint32_t kGate = 0;         // 3 gate digit planes + a zero plane, 64 rows x 128 B each
+    static constexpr uint32_t kGateBytes = kUmmaGatePlaneBytes64;
+    static constexpr uint32_t kPlanes = 0;       // (state planes all in tensor memory)
+    static constexpr uint32_t kTile0 = 32768;    // tile buffers, 4096 x float2
+    static constexpr uint32_t kTile1 = 65536;
+    static constexpr uint32_t kTileBytes = 4096 * 8;
+    static constexpr uint32_t kEcol = 98304;
+    static constexpr uint32_t kTmPlanes = 256;   // four level regions of 64, then planes 0-2
+    static constexpr uint32_t kTabEntry = 8;     // factor-table entry: FP32 complex
+};
+template <bool C64>
+struct Sm : Lay<C64> {
+    using L = Lay<C64>;
+    static constexpr uint32_t kEcol = L::kEcol;   // int[64]: gate column exponents
+    static constexpr uint32_t kErow = kEcol + 256;  // int[128]: group exponents of the current tile
+    static constexpr uint32_t kMx = kErow + 512;    // uint32[512]: quarter-group maxima
+    static constexpr uint32_t kGb = kMx + 2048;     // uint16[128]: tile index of each group's input 0
+    static constexpr uint32_t kOff = kGb + 256;     // uint16[32]: tile offset of each input
+    static constexpr uint32_t kBar = kOff + 64;     // 6 mbarriers
+    static constexpr uint32_t kMisc = kBar + 64;    // tensor-memory base, abort flag
+    static constexpr uint32_t kLut = kMisc + 64;    // uint8[2][2][64]: factor-table index of tile slots 0-5 / 6-11
+    static constexpr uint32_t kTab = kLut + 256;    // [2][256] factor tables of the current tile
+    static constexpr uint32_t kEw = kTab + 2 * (1u << kUmmaRunBits) * L::kTabEntry;  // element-wise matrices
+    static constexpr uint32_t kBytes = kEw + kUmmaEwMaxBytes + 1024;  // + alignment slack
+};
 
-// tensor-memory columns: six level regions of 64, then state planes 0-3
 constexpr uint32_t kTmemCols = 512;
-constexpr uint32_t kTmPlanes = 384;
-
-constexpr uint32_t kTileBytes = 4096 * 16;
 
 __device__ __forceinline__ uint64_t insert_zero_u(uint64_t v, int p) {
     const uint64_t low = v & ((1ULL << p) - 1ULL);
@@ -289,29 +316,94 @@ __device__ __forceinline__ void run_apply(double2* buf, const float4* tab, const
     }
 }
 
+// ------------------------------------------------------------------ complex64
+// The complex64 instance writes every state real as three balanced base-2^9
+// digits relative to its group's largest float exponent Ef (X' = x 2^k,
+// k = min(134 - Ef, 126), |X'| < 2^8: d0 = X' rounded to an integer, then two
+// more rounded 9-bit digits, X' to 2^-19, 2^-27 of the group's scale), every
+// gate real as three digits relative to its column (|B'| < 2^7, top digit
+// <= 128). The products with i + j = 0..3 go to four FP32 accumulator
+// regions; every level sum stays below 2^24 (level 2, the largest:
+// 64 (256^2 + 256^2 + 256 * 128) < 2^23.4), so the accumulators hold exact
+// integers and the tensor cores' rounding of their accumulation never
+// applies. The dropped level 4 (d2 e2) is below 2^-34 of the
+// row-times-column scale. The output is sum_L S_L 2^(-9 L) by an FMA chain
+// (error below 2^-23 of sum_k |x_k b_kn|), times the column's and the
+// group's scale.
+
+// X' = x 2^k; each digit rounds with the magic-number add folded into an FMA
+// (the product by 512 is exact, so the FMA rounds once, to an integer)
+__device__ __forceinline__ void digits3(float x, float sk, float (&dg)[3]) {
+    const float X = __fmul_rn(x, sk);
+    dg[0] = __fsub_rn(__fadd_rn(X, kMagic0), kMagic0);
+    const float r = __fsub_rn(X, dg[0]);
+    dg[1] = __fsub_rn(__fmaf_rn(r, 512.f, kMagic0), kMagic0);
+    const float u = __fmaf_rn(r, 512.f, -dg[1]);
+    dg[2] = __fsub_rn(__fmaf_rn(u, 512.f, kMagic0), kMagic0);
+}
+
+// sum_L S_L 2^(-9 L) for the four exact level sums
+__device__ __forceinline__ float level_sum4(const float (&S)[4]) {
+    const float t = __fmaf_rn(S[2], 1.0f / 262144.f, __fmul_rn(S[3], 1.0f / 134217728.f));
+    return __fadd_rn(S[0], __fmaf_rn(S[1], 1.0f / 512.f, t));
+}
+
+// run_entry for complex64: FP32 complex products of the run's entries
+__device__ __forceinline__ float2 run_entry64(const float2* __restrict__ pool, const PassDesc& d, int o0, int o1,
+                                              uint32_t mask, uint32_t i, uint64_t base) {
+    uint32_t L = 0;
+    for (int sl = 0; sl < 12; ++sl)
+        if ((mask >> sl) & 1u) {
+            L |= (i & 1u) << sl;
+            i >>= 1;
+        }
+    float2 x = make_float2(1.f, 0.f);
+    for (int o = o0; o < o1; ++o) {
+        const OpDesc& op = d.ops[o];
+        if ((base & op.ctrl_outer) != op.ctrl_outer) continue;
+        if (op.k == 0) {
+            x = ArithF32::mul(pool[op.mat_off], x);
+            continue;
+        }
+        if ((L & op.ctrl_local) != op.ctrl_local) continue;
+        int r = 0;
+        for (int j = 0; j < op.k; ++j) {
+            const int sl = op.tslot[j];
+            const uint64_t bit = (sl & kOuterSlot) ? (base >> (sl & 63)) : ((uint64_t)L >> sl);
+            r |= (int)(bit & 1ULL) << j;
+        }
+        x = ArithF32::mul(pool[op.mat_off + r], x);
+    }
+    return x;
+}
+
+__device__ __forceinline__ void run_apply64(float2* buf, const float2* tab, const uint8_t* lut) {
+    for (int L = threadIdx.x; L < 4096; L += kCompute) buf[L] = ArithF32::mul(tab[run_index(lut, (uint32_t)L)], buf[L]);
+}
+
 // ------------------------------------------------------------------ kernel
+template <bool C64>
 __global__ void __launch_bounds__(kThreadsU, 1)
     umma_pass_kernel(const __grid_constant__ CUtensorMap tmap, const __grid_constant__ UmmaDesc u,
                      const unsigned char* __restrict__ pool, int* __restrict__ err) {
+    using S = Sm<C64>;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* sm = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
     const PassDesc& d = u.d;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + kSmBar);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + S::kBar);
     uint64_t* full = bars;        // [2] tile loaded
     uint64_t* tdone = bars + 2;   // [2] tile computed
     uint64_t* pbar = bars + 4;    // state digits written
     uint64_t* mbar = bars + 5;    // MMAs complete
-    uint32_t* tmem_s = reinterpret_cast<uint32_t*>(sm + kSmMisc);
-    volatile int* abort = reinterpret_cast<volatile int*>(sm + kSmMisc + 8);
-    int* erow = reinterpret_cast<int*>(sm + kSmErow);
-    const int* ecol = reinterpret_cast<const int*>(sm + kSmEcol);
-    uint32_t* mxs = reinterpret_cast<uint32_t*>(sm + kSmMx);
-    uint16_t* gb = reinterpret_cast<uint16_t*>(sm + kSmGb);
-    uint16_t* offt = reinterpret_cast<uint16_t*>(sm + kSmOff);
-    const float4* ewp = reinterpret_cast<const float4*>(sm + kSmEw);
-    uint8_t* lut = sm + kSmLut;
-    float4* tab = reinterpret_cast<float4*>(sm + kSmTab);
+    uint32_t* tmem_s = reinterpret_cast<uint32_t*>(sm + S::kMisc);
+    volatile int* abort = reinterpret_cast<volatile int*>(sm + S::kMisc + 8);
+    int* erow = reinterpret_cast<int*>(sm + S::kErow);
+    const int* ecol = reinterpret_cast<const int*>(sm + S::kEcol);
+    uint32_t* mxs = reinterpret_cast<uint32_t*>(sm + S::kMx);
+    uint16_t* gb = reinterpret_cast<uint16_t*>(sm + S::kGb);
+    uint16_t* offt = reinterpret_cast<uint16_t*>(sm + S::kOff);
+    uint8_t* lut = sm + S::kLut;
 
     const uint64_t ntiles = 1ULL << (d.n - d.nins);
     const uint64_t my_n = (uint64_t)blockIdx.x < ntiles ? (ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x : 0;
@@ -325,14 +417,25 @@ __global__ void __launch_bounds__(kThreadsU, 1)
     if (warp == kMmaWarp) tmem_alloc(tmem_s, kTmemCols);
     if (threadIdx.x < kCompute) {
         const uint4* gsrc = reinterpret_cast<const uint4*>(pool + u.gate_off);
-        uint4* gdst = reinterpret_cast<uint4*>(sm + kSmGate);
-        for (int i = threadIdx.x; i < (int)(kUmmaGatePlaneBytes / 16); i += kCompute) gdst[i] = gsrc[i];
-        if (threadIdx.x < 64)
-            reinterpret_cast<int*>(sm + kSmEcol)[threadIdx.x] =
-                reinterpret_cast<const int*>(pool + u.gate_off + kUmmaGatePlaneBytes)[threadIdx.x];
+        uint4* gdst = reinterpret_cast<uint4*>(sm + S::kGate);
+        for (int i = threadIdx.x; i < (int)(S::kGateBytes / 16); i += kCompute) gdst[i] = gsrc[i];
+        if (threadIdx.x < 64) {
+            const int ec = reinterpret_cast<const int*>(pool + u.gate_off + S::kGateBytes)[threadIdx.x];
+            if constexpr (C64) {
+                // the column's scale 2^(ec - 1029) as a float (subnormal or 0
+                // for columns far below 1; a unitary's columns are not)
+                const int e = ec - 1029;
+                const uint32_t bits = e >= -126 ? (uint32_t)(e + 127) << 23 : e >= -149 ? 1u << (e + 149) : 0u;
+                reinterpret_cast<float*>(sm + S::kEcol)[threadIdx.x] = __uint_as_float(bits);
+            } else {
+                reinterpret_cast<int*>(sm + S::kEcol)[threadIdx.x] = ec;
+            }
+        }
         const uint4* esrc = reinterpret_cast<const uint4*>(pool);
-        uint4* edst = reinterpret_cast<uint4*>(sm + kSmEw);
-        for (int i = threadIdx.x; i < (int)(u.ew_bytes / 16); i += kCompute) edst[i] = esrc[i];
+        uint4* edst = reinterpret_cast<uint4*>(sm + S::kEw);
+        // whole 16-byte chunks (complex64 entries are 8 bytes; the pool's
+        // element-wise block is padded to the gate block's 1024-byte offset)
+        for (int i = threadIdx.x; i < (int)((u.ew_bytes + 15) / 16); i += kCompute) edst[i] = esrc[i];
         // group g's first tile index: g's bits deposited over the slots that
         // are not targets; input e's offset: e's bits over the target slots
         uint32_t tmask = 0;
@@ -375,9 +478,9 @@ __global__ void __launch_bounds__(kThreadsU, 1)
         const uint32_t ncopy = 1u << u.nextra;
         uint32_t issued[2] = {0, 0};
         auto load = [&](uint64_t b, int s) {
-            unsigned char* buf = sm + (s ? kSmTile1 : kSmTile0);
+            unsigned char* buf = sm + (s ? S::kTile1 : S::kTile0);
             if (lane == 0) {
-                mbar_arrive_expect_tx(&full[s], kTileBytes);
+                mbar_arrive_expect_tx(&full[s], S::kTileBytes);
                 for (uint32_t c = 0; c < ncopy; ++c) {
                     int32_t co[5];
                     tile_coords(u, b, c, co);
@@ -404,7 +507,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
             if (!ok) break;
             if (lane == 0) {
-                const unsigned char* buf = sm + (s ? kSmTile1 : kSmTile0);
+                const unsigned char* buf = sm + (s ? S::kTile1 : S::kTile0);
                 for (uint32_t c = 0; c < ncopy; ++c) {
                     int32_t co[5];
                     tile_coords(u, sb, c, co);
@@ -432,7 +535,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
         // ---- MMA issue
         const uint32_t idesc256 = idesc_f16(128, 256), idesc192 = idesc_f16(128, 192),
                        idesc128 = idesc_f16(128, 128), idesc64 = idesc_f16(128, 64);
-        const uint32_t gate = smem_u32(sm + kSmGate), planes = smem_u32(sm + kSmPlanes);
+        const uint32_t gate = smem_u32(sm + S::kGate), planes = smem_u32(sm + S::kPlanes);
         uint64_t committed = 0;
         for (uint64_t it = 0; it < my_n; ++it) {
             bool ok = true;
@@ -445,19 +548,26 @@ __global__ void __launch_bounds__(kThreadsU, 1)
                 for (int ks = 0; ks < 4; ++ks) {
                     // X_i times gate digits j0.. accumulates at level region i + j0
                     auto gdesc = [&](int j0) { return sdesc_sw128(gate + (uint32_t)j0 * 8192u + (uint32_t)ks * 32u); };
-                    auto ta = [&](int i) { return tmem + kTmPlanes + (uint32_t)i * 32u + (uint32_t)ks * 8u; };
+                    auto ta = [&](int i) { return tmem + S::kTmPlanes + (uint32_t)i * 32u + (uint32_t)ks * 8u; };
                     auto td = [&](int lev) { return tmem + (uint32_t)lev * 64u; };
                     const uint32_t acc0 = ks > 0 ? 1u : 0u;
-                    mma_ts(td(0), ta(0), gdesc(0), idesc256, acc0);  // levels 0-3
-                    mma_ts(td(4), ta(0), gdesc(4), idesc128, acc0);  // levels 4-5
-                    mma_ts(td(1), ta(1), gdesc(0), idesc256, 1u);    // levels 1-4
-                    mma_ts(td(5), ta(1), gdesc(4), idesc64, 1u);     // level 5
-                    mma_ts(td(2), ta(2), gdesc(0), idesc256, 1u);    // levels 2-5
-                    mma_ts(td(3), ta(3), gdesc(0), idesc192, 1u);    // levels 3-5
-                    const uint64_t a4 = sdesc_sw128(planes + (uint32_t)ks * 32u);
-                    const uint64_t a5 = sdesc_sw128(planes + 16384u + (uint32_t)ks * 32u);
-                    mma_ss(td(4), a4, gdesc(0), idesc128, 1u);       // levels 4-5
-                    mma_ss(td(5), a5, gdesc(0), idesc64, 1u);        // level 5
+                    if constexpr (C64) {
+                        // gate plane 3 is zero: the first MMA also clears level 3
+                        mma_ts(td(0), ta(0), gdesc(0), idesc256, acc0);  // levels 0-3
+                        mma_ts(td(1), ta(1), gdesc(0), idesc192, 1u);    // levels 1-3
+                        mma_ts(td(2), ta(2), gdesc(0), idesc128, 1u);    // levels 2-3
+                    } else {
+                        mma_ts(td(0), ta(0), gdesc(0), idesc256, acc0);  // levels 0-3
+                        mma_ts(td(4), ta(0), gdesc(4), idesc128, acc0);  // levels 4-5
+                        mma_ts(td(1), ta(1), gdesc(0), idesc256, 1u);    // levels 1-4
+                        mma_ts(td(5), ta(1), gdesc(4), idesc64, 1u);     // level 5
+                        mma_ts(td(2), ta(2), gdesc(0), idesc256, 1u);    // levels 2-5
+                        mma_ts(td(3), ta(3), gdesc(0), idesc192, 1u);    // levels 3-5
+                        const uint64_t a4 = sdesc_sw128(planes + (uint32_t)ks * 32u);
+                        const uint64_t a5 = sdesc_sw128(planes + 16384u + (uint32_t)ks * 32u);
+                        mma_ss(td(4), a4, gdesc(0), idesc128, 1u);       // levels 4-5
+                        mma_ss(td(5), a5, gdesc(0), idesc64, 1u);        // level 5
+                    }
                 }
                 mma_commit(mbar);
             }
@@ -469,8 +579,8 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             mbar_wait_quiet(mbar, (uint32_t)((committed - 1) & 1));
         }
         __syncwarp();
-    } else {
-        // ---- compute warps: digits, then outputs. The runs' factor tables
+    } else if constexpr (!C64) {
+        // ---- compute warps (complex128): digits, then outputs. The runs' factor tables
         // are built while the MMAs of the tile run: the post-run table of
         // this tile and the pre-run table of the next (the pre-run table of
         // the first tile before the loop). A pre-run is applied while the
@@ -481,8 +591,9 @@ __global__ void __launch_bounds__(kThreadsU, 1)
         const uint32_t lane_base = (uint32_t)(q4 * 32) << 16;
         const bool pre = u.tc_op > 0, post = u.tc_op + 1 < d.nops;
         const int npre = pre ? 1 << __popc(u.run_mask[0]) : 0, npost = post ? 1 << __popc(u.run_mask[1]) : 0;
-        float4* tab_pre = tab;
-        float4* tab_post = tab + (1 << kUmmaRunBits);
+        float4* tab_pre = reinterpret_cast<float4*>(sm + S::kTab);
+        float4* tab_post = tab_pre + (1 << kUmmaRunBits);
+        const float4* ewp = reinterpret_cast<const float4*>(sm + S::kEw);
         const uint8_t* lut_pre = lut;
         const uint8_t* lut_post = lut + 128;
         auto build_pre = [&](uint64_t b) {
@@ -498,7 +609,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
         if (my_n > 0) build_pre(base);
         for (uint64_t it = 0; it < my_n; ++it, base = walk.after(base)) {
             const int s = (int)(it & 1);
-            double2* buf = reinterpret_cast<double2*>(sm + (s ? kSmTile1 : kSmTile0));
+            double2* buf = reinterpret_cast<double2*>(sm + (s ? S::kTile1 : S::kTile0));
             mbar_wait(&full[s], (uint32_t)((it >> 1) & 1), abort);
             bar_sync(1, kCompute);
             if (*abort) break;
@@ -540,11 +651,11 @@ __global__ void __launch_bounds__(kThreadsU, 1)
                         const uint32_t e0 = (uint32_t)(part * 8 + bt * 4);
 #pragma unroll
                         for (int q = 0; q < 4; ++q)
-                            tmem_st4(tmem + lane_base + kTmPlanes + (uint32_t)q * 32u + e0, pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
+                            tmem_st4(tmem + lane_base + S::kTmPlanes + (uint32_t)q * 32u + e0, pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
                         const uint32_t c0 = e0 >> 2;
 #pragma unroll
                         for (int q = 4; q < 6; ++q) {
-                            unsigned char* row = sm + kSmPlanes + (uint32_t)(q - 4) * 16384u + (uint32_t)g * 128u;
+                            unsigned char* row = sm + S::kPlanes + (uint32_t)(q - 4) * 16384u + (uint32_t)g * 128u;
                             *reinterpret_cast<uint4*>(row + ((c0 ^ (g & 7)) << 4)) =
                                 make_uint4(pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
                         }
@@ -575,11 +686,11 @@ __global__ void __launch_bounds__(kThreadsU, 1)
                         const uint32_t e0 = (uint32_t)(part * 8 + bt * 4);
 #pragma unroll
                         for (int q = 0; q < 4; ++q)
-                            tmem_st4(tmem + lane_base + kTmPlanes + (uint32_t)q * 32u + e0, pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
+                            tmem_st4(tmem + lane_base + S::kTmPlanes + (uint32_t)q * 32u + e0, pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
                         const uint32_t c0 = e0 >> 2;
 #pragma unroll
                         for (int q = 4; q < 6; ++q) {
-                            unsigned char* row = sm + kSmPlanes + (uint32_t)(q - 4) * 16384u + (uint32_t)g * 128u;
+                            unsigned char* row = sm + S::kPlanes + (uint32_t)(q - 4) * 16384u + (uint32_t)g * 128u;
                             *reinterpret_cast<uint4*>(row + ((c0 ^ (g & 7)) << 4)) =
                                 make_uint4(pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
                         }
@@ -652,6 +763,133 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             bar_sync(1, kCompute);
             if (threadIdx.x == 0) mbar_arrive(&tdone[s]);
         }
+    } else {
+        // ---- compute warps (complex64): three digits per real (exact
+        // levels 0-3), runs in FP32 complex, outputs rounded to float
+        const int q4 = warp & 3, part = warp >> 2, g = q4 * 32 + lane;
+        const OpDesc& tc = d.ops[u.tc_op];
+        const uint32_t lane_base = (uint32_t)(q4 * 32) << 16;
+        const bool pre = u.tc_op > 0, post = u.tc_op + 1 < d.nops;
+        const int npre = pre ? 1 << __popc(u.run_mask[0]) : 0, npost = post ? 1 << __popc(u.run_mask[1]) : 0;
+        float2* tab_pre = reinterpret_cast<float2*>(sm + S::kTab);
+        float2* tab_post = tab_pre + (1 << kUmmaRunBits);
+        const float2* ewp = reinterpret_cast<const float2*>(sm + S::kEw);
+        const uint8_t* lut_pre = lut;
+        const uint8_t* lut_post = lut + 128;
+        auto build_pre = [&](uint64_t b) {
+            for (int i = threadIdx.x; i < npre; i += kCompute)
+                tab_pre[i] = run_entry64(ewp, d, 0, u.tc_op, u.run_mask[0], (uint32_t)i, b);
+        };
+        auto build_post = [&](uint64_t b) {
+            for (int i = threadIdx.x; i < npost; i += kCompute)
+                tab_post[i] = run_entry64(ewp, d, u.tc_op + 1, d.nops, u.run_mask[1], (uint32_t)i, b);
+        };
+        const Walk walk(d, blockIdx.x, gridDim.x);
+        uint64_t base = walk.base;
+        if (my_n > 0) build_pre(base);
+        for (uint64_t it = 0; it < my_n; ++it, base = walk.after(base)) {
+            const int s = (int)(it & 1);
+            float2* buf = reinterpret_cast<float2*>(sm + (s ? S::kTile1 : S::kTile0));
+            mbar_wait(&full[s], (uint32_t)((it >> 1) & 1), abort);
+            bar_sync(1, kCompute);
+            if (*abort) break;
+            const bool act = (base & tc.ctrl_outer) == tc.ctrl_outer;
+            const uint32_t gbase = gb[g];
+            const bool write = (gbase & tc.ctrl_local) == tc.ctrl_local;
+            if (act) {
+                // group g, inputs 8 part .. 8 part + 7 (the pre-run applied)
+                float2 xv[8];
+                float mx = 0.f;
+#pragma unroll
+                for (int i = 0; i < 8; ++i) {
+                    const uint32_t L = gbase | offt[part * 8 + i];
+                    float2 v = buf[L];
+                    if (pre) {
+                        v = ArithF32::mul(tab_pre[run_index(lut_pre, L)], v);
+                        if (!write) buf[L] = v;
+                    }
+                    xv[i] = v;
+                    mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+                }
+                reinterpret_cast<float*>(mxs)[threadIdx.x] = mx;
+                bar_sync(1, kCompute);
+                const float* mxf = reinterpret_cast<const float*>(mxs);
+                const int Ef = (int)(__float_as_uint(fmaxf(fmaxf(mxf[g], mxf[128 + g]), fmaxf(mxf[256 + g], mxf[384 + g]))) >> 23);
+                // X' = x 2^k; the group's output scale is 2^-k (0: all zero)
+                const int k = min(134 - Ef, 126);
+                if (part == 0) erow[g] = Ef == 0 ? 0 : 127 - k;
+                const float sk = __uint_as_float((uint32_t)(k + 127) << 23);
+#pragma unroll
+                for (int bt = 0; bt < 2; ++bt) {
+                    uint32_t pl[3][4];
+#pragma unroll
+                    for (int i = 0; i < 4; ++i) {
+                        float dr[3], di[3];
+                        digits3(xv[bt * 4 + i].x, sk, dr);
+                        digits3(xv[bt * 4 + i].y, sk, di);
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) pl[q][i] = pack_h2(dr[q], di[q]);
+                    }
+                    const uint32_t e0 = (uint32_t)(part * 8 + bt * 4);
+#pragma unroll
+                    for (int q = 0; q < 3; ++q)
+                        tmem_st4(tmem + lane_base + S::kTmPlanes + (uint32_t)q * 32u + e0, pl[q][0], pl[q][1], pl[q][2], pl[q][3]);
+                }
+                tmem_st_wait();
+            } else if (pre) {
+                run_apply64(buf, tab_pre, lut_pre);
+            }
+            fence_before_sync();
+            bar_sync(1, kCompute);
+            if (threadIdx.x == 0) mbar_arrive(pbar);
+            // while the MMAs run: this tile's post-run table, the next tile's pre-run table
+            if (post) build_post(base);
+            if (pre && it + 1 < my_n) build_pre(walk.after(base));
+            mbar_wait(mbar, (uint32_t)(it & 1), abort);
+            bar_sync(1, kCompute);
+            if (*abort) break;
+            fence_after_sync();
+            if (act) {
+                // outputs: group g, output reals 16 part .. 16 part + 15; the
+                // tensor-memory loads are warp-collective (every thread takes part)
+                const int gexp = erow[g];
+                const float gs = __uint_as_float((uint32_t)gexp << 23);  // 0 for a zero group
+                const float* cs = reinterpret_cast<const float*>(sm + S::kEcol);
+#pragma unroll
+                for (int ch = 0; ch < 2; ++ch) {
+                    const uint32_t n0 = (uint32_t)(part * 16 + ch * 8);
+                    uint32_t r[4][8];
+#pragma unroll
+                    for (int lev = 0; lev < 4; ++lev) tmem_ld8(tmem + lane_base + (uint32_t)lev * 64u + n0, r[lev]);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int a = 0; a < 4; ++a) {
+                        const uint32_t L = gbase | offt[(n0 >> 1) + a];
+                        if (!write) {  // the pre-run was stored with the digits
+                            if (post) buf[L] = ArithF32::mul(tab_post[run_index(lut_post, L)], buf[L]);
+                            continue;
+                        }
+                        float y[2];
+#pragma unroll
+                        for (int p = 0; p < 2; ++p) {
+                            const int c = a * 2 + p;
+                            const float Sl[4] = {__uint_as_float(r[0][c]), __uint_as_float(r[1][c]),
+                                                 __uint_as_float(r[2][c]), __uint_as_float(r[3][c])};
+                            y[p] = __fmul_rn(__fmul_rn(level_sum4(Sl), cs[n0 + c]), gs);
+                        }
+                        float2 v = make_float2(y[0], y[1]);
+                        if (post) v = ArithF32::mul(tab_post[run_index(lut_post, L)], v);
+                        buf[L] = v;
+                    }
+                }
+            } else if (post) {
+                run_apply64(buf, tab_post, lut_post);
+            }
+            fence_proxy_async();
+            fence_before_sync();
+            bar_sync(1, kCompute);
+            if (threadIdx.x == 0) mbar_arrive(&tdone[s]);
+        }
     }
 
     // ---- tear-down
@@ -683,7 +921,7 @@ EncodeTiledFn encode_fn() {
 constexpr int kMaxDev = 64;
 std::mutex g_umma_mu;
 int* g_err_word[kMaxDev] = {nullptr};
-bool g_attr_set[kMaxDev] = {false};
+bool g_attr_set[kMaxDev][2] = {};
 
 int current_device() {
     int dev = 0;
@@ -693,29 +931,33 @@ int current_device() {
 
 }  // namespace
 
-size_t umma_smem_bytes() { return kSmBytes; }
+size_t umma_smem_bytes() { return Sm<false>::kBytes; }
 
 cudaError_t launch_umma_pass(void* state, const void* mats, const UmmaDesc& u, cudaStream_t s) {
     EncodeTiledFn enc = encode_fn();
     if (!enc) return cudaErrorNotSupported;
-    // the state viewed as doubles: each dimension spans dim_bits state
-    // positions from dim_pos (dimension 0 also the re/im pair)
+    const bool c64 = u.c64 != 0;
+    // the state viewed as reals (doubles, or floats for complex64): each
+    // dimension spans dim_bits state positions from dim_pos (dimension 0
+    // also the re/im pair), its box the dim_box positions at its bottom
+    const uint64_t amp = c64 ? 8 : 16;
     cuuint64_t gdim[5], gstr[4];
     cuuint32_t box[5], es[5];
     for (int i = 0; i < u.rank; ++i) {
         gdim[i] = (i == 0 ? 2ULL : 1ULL) << u.dim_bits[i];
         box[i] = (i == 0 ? 2u : 1u) << u.dim_box[i];
         es[i] = 1;
-        if (i > 0) gstr[i - 1] = 16ULL << u.dim_pos[i];
+        if (i > 0) gstr[i - 1] = amp << u.dim_pos[i];
     }
     CUtensorMap tm;
-    const CUresult r = enc(&tm, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, (cuuint32_t)u.rank, state, gdim,
-                           u.rank > 1 ? gstr : nullptr, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                           CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+    const CUresult r = enc(&tm, c64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                           (cuuint32_t)u.rank, state, gdim, u.rank > 1 ? gstr : nullptr, box, es,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return cudaErrorInvalidValue;
     const int dev = current_device();
     if (dev < 0) return cudaErrorInvalidDevice;
+    const uint32_t smem = c64 ? Sm<true>::kBytes : Sm<false>::kBytes;
     int* err = nullptr;
     {
         std::lock_guard<std::mutex> lk(g_umma_mu);
@@ -725,17 +967,22 @@ cudaError_t launch_umma_pass(void* state, const void* mats, const UmmaDesc& u, c
             e = cudaMemset(g_err_word[dev], 0, sizeof(int));
             if (e != cudaSuccess) return e;
         }
-        if (!g_attr_set[dev]) {
-            cudaError_t e =
-                cudaFuncSetAttribute(umma_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmBytes);
+        if (!g_attr_set[dev][c64 ? 1 : 0]) {
+            cudaError_t e = c64 ? cudaFuncSetAttribute(umma_pass_kernel<true>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)
+                                : cudaFuncSetAttribute(umma_pass_kernel<false>,
+                                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
-            g_attr_set[dev] = true;
+            g_attr_set[dev][c64 ? 1 : 0] = true;
         }
         err = g_err_word[dev];
     }
     const uint64_t ntiles = 1ULL << (u.d.n - u.d.nins);
     const unsigned grid = (unsigned)std::min<uint64_t>(ntiles, (uint64_t)device_sm_count());
-    umma_pass_kernel<<<grid, kThreadsU, kSmBytes, s>>>(tm, u, static_cast<const unsigned char*>(mats), err);
+    if (c64)
+        umma_pass_kernel<true><<<grid, kThreadsU, smem, s>>>(tm, u, static_cast<const unsigned char*>(mats), err);
+    else
+        umma_pass_kernel<false><<<grid, kThreadsU, smem, s>>>(tm, u, static_cast<const unsigned char*>(mats), err);
     return cudaGetLastError();
 }
 

@@ -491,39 +491,42 @@ bool umma_enabled() {
 }
 
 bool umma_candidate(int arith, const GateOp& op) {
-    return arith == kArithTC && !op.diag && op.k >= 3 && op.k <= 5;
+    return (arith == kArithTC || arith == kArithTC64) && !op.diag && op.k >= 3 && op.k <= 5;
 }
 
 static bool elementwise_op(const GateOp& op) { return op.k == 0 || op.diag; }
 
-// double-float matrix entries (16 B each) of an element-wise op
-static size_t ew_pool_bytes(const GateOp& op) { return op.m.size() * 16; }
+// matrix entries of an element-wise op in a tensor-memory pass: double-float
+// complex (16 B) for complex128 states, FP32 complex (8 B) for complex64
+static size_t ew_pool_bytes(const GateOp& op, int arith) { return op.m.size() * (arith == kArithTC64 ? 8 : 16); }
 
 // The six balanced base-2^9 digits of a gate real v relative to its column's
 // largest biased exponent ebmax, with the column scaled to |v'| < 2^7:
 // a = rint(|v| 2^(1074 - ebmax)) (to nearest, ties to even; a < 2^52) cut
 // into 9-bit fields, balanced into [-256, 255] with carries upward (the top
 // digit ends at most 128), then given v's sign.
-static void gate_digits9(double v, int ebmax, int (&d)[6]) {
+// With nd = 3 (complex64) the same column scale keeps the top three digits:
+// a = rint(|v| 2^(1047 - ebmax)) < 2^25.
+static void gate_digits9(double v, int ebmax, int nd, int (&d)[6]) {
     uint64_t u;
     std::memcpy(&u, &v, 8);
     const int eb = (int)((u >> 52) & 0x7FF);
     uint64_t a = 0;
-    const int sh = ebmax - eb + 1;
+    const int sh = ebmax - eb + 1 + 9 * (6 - nd);
     if (eb != 0 && sh < 62) {
         const uint64_t M = (u & 0xFFFFFFFFFFFFFULL) | (1ULL << 52);
         a = (M + (1ULL << (sh - 1)) - 1ULL + ((M >> sh) & 1ULL)) >> sh;
     }
     int r[6];
-    for (int i = 1; i < 6; ++i) r[i] = (int)((a >> (9 * (5 - i))) & 511u);
-    r[0] = (int)(a >> 45);
-    for (int i = 5; i >= 1; --i) {
+    for (int i = 1; i < nd; ++i) r[i] = (int)((a >> (9 * (nd - 1 - i))) & 511u);
+    r[0] = (int)(a >> (9 * (nd - 1)));
+    for (int i = nd - 1; i >= 1; --i) {
         const int c = (r[i] + 256) >> 9;
         r[i] -= c << 9;
         r[i - 1] += c;
     }
     const bool neg = (u >> 63) != 0;
-    for (int i = 0; i < 6; ++i) d[i] = neg ? -r[i] : r[i];
+    for (int i = 0; i < 6; ++i) d[i] = i >= nd ? 0 : neg ? -r[i] : r[i];
 }
 
 // Gate block of a tensor-memory pass: the gate widened to the five target
@@ -531,8 +534,9 @@ static void gate_digits9(double v, int ebmax, int (&d)[6]) {
 // that are not the gate's targets), in real form B[k][n] (k = 2c + part of
 // input c, n = 2r + part of output r), as six digit planes (plane j: rows
 // n = 0..63 of 64 fp16 over k, K-major with the 128-byte swizzle of the MMA
-// operand), then the 64 column exponents as int32.
-static void build_umma_gate(const GateOp& g, const int (&pos5)[5], unsigned char* dst) {
+// operand), then the 64 column exponents as int32. complex64: three digit
+// planes and a fourth of zeros.
+static void build_umma_gate(const GateOp& g, const int (&pos5)[5], bool c64, unsigned char* dst) {
     int realbit[5];
     for (int j = 0; j < 5; ++j) {
         realbit[j] = -1;
@@ -559,17 +563,19 @@ static void build_umma_gate(const GateOp& g, const int (&pos5)[5], unsigned char
         if (pin == 0) return pout == 0 ? m.real() : m.imag();
         return pout == 0 ? -m.imag() : m.real();
     };
+    const uint32_t plane_bytes = c64 ? kUmmaGatePlaneBytes64 : kUmmaGatePlaneBytes;
+    const int nd = c64 ? 3 : 6;
     uint16_t* planes = reinterpret_cast<uint16_t*>(dst);
-    std::memset(planes, 0, kUmmaGatePlaneBytes);
-    int32_t* ecol = reinterpret_cast<int32_t*>(dst + kUmmaGatePlaneBytes);
+    std::memset(planes, 0, plane_bytes);
+    int32_t* ecol = reinterpret_cast<int32_t*>(dst + plane_bytes);
     for (int nn = 0; nn < 64; ++nn) {
         int ebmax = 0;
         for (int kk = 0; kk < 64; ++kk) ebmax = std::max(ebmax, biased_exponent(bval(kk, nn)));
         ecol[nn] = ebmax;
         for (int kk = 0; kk < 64; ++kk) {
             int dg[6];
-            gate_digits9(bval(kk, nn), ebmax, dg);
-            for (int j = 0; j < 6; ++j) {
+            gate_digits9(bval(kk, nn), ebmax, nd, dg);
+            for (int j = 0; j < nd; ++j) {
                 const int row = 64 * j + nn;
                 const size_t byte = (size_t)row * 128 + ((size_t)(((2 * kk) >> 4) ^ (row & 7)) << 4) + ((2 * kk) & 15);
                 planes[byte / 2] = half_of_int(dg[j]);
@@ -586,7 +592,8 @@ static void build_umma_gate(const GateOp& g, const int (&pos5)[5], unsigned char
 // depends on too many tile slots, or another reason (state too small,
 // element-wise matrices too large).
 enum { kUmmaOk = 0, kUmmaPreWide = 1, kUmmaPostWide = 2, kUmmaNo = 3 };
-static int build_umma(int n, const GateOp* ops, size_t i0, size_t tc, size_t i1, UmmaDesc& u, uint64_t& bytes) {
+static int build_umma(int n, int arith, const GateOp* ops, size_t i0, size_t tc, size_t i1, UmmaDesc& u,
+                      uint64_t& bytes) {
     const GateOp& g = ops[tc];
     uint64_t tmask = 0;
     for (int t = 0; t < g.k; ++t) tmask |= 1ULL << g.pos[t];
@@ -606,10 +613,11 @@ static int build_umma(int n, const GateOp* ops, size_t i0, size_t tc, size_t i1,
     for (int p : picks) tile |= 1ULL << p;
     size_t ewb = 0;
     for (size_t o = i0; o < i1; ++o)
-        if (o != tc) ewb += ew_pool_bytes(ops[o]);
+        if (o != tc) ewb += ew_pool_bytes(ops[o], arith);
     if (ewb > kUmmaEwMaxBytes || i1 - i0 > (size_t)kMaxOpsPerPass) return kUmmaNo;
 
     std::memset(&u, 0, sizeof(u));
+    u.c64 = arith == kArithTC64 ? 1 : 0;
     PassDesc& d = u.d;
     int slot[64];
     int c = 0;
@@ -709,8 +717,9 @@ static int build_umma(int n, const GateOp* ops, size_t i0, size_t tc, size_t i1,
     }
     u.rank = (uint8_t)rank;
     if (tbits + u.nextra != kUmmaTileBits) return kUmmaNo;
-    u.box_bytes = 16u << tbits;
-    bytes = 2ULL * (1ULL << (n - popc64(fixed))) * 16;
+    const uint32_t amp = u.c64 ? 8u : 16u;
+    u.box_bytes = amp << tbits;
+    bytes = 2ULL * (1ULL << (n - popc64(fixed))) * amp;
     return kUmmaOk;
 }
 
@@ -718,13 +727,18 @@ void write_umma_pool(const UmmaDesc& u, const GateOp* ops, unsigned char* dst) {
     const PassDesc& d = u.d;
     for (int o = 0; o < d.nops; ++o) {
         if (o == u.tc_op) continue;
-        // element-wise matrices in double-float (the tensor-core arithmetic's
-        // matrix format), untransposed
+        // element-wise matrices, untransposed: double-float complex for a
+        // complex128 state, FP32 complex for complex64
         const GateOp& op = ops[o];
-        float* p = reinterpret_cast<float*>(dst + (size_t)d.ops[o].mat_off * 16);
+        float* p = reinterpret_cast<float*>(dst + (size_t)d.ops[o].mat_off * (u.c64 ? 8 : 16));
         for (size_t e = 0; e < op.m.size(); ++e) {
             const double re = op.m[e].real(), im = op.m[e].imag();
             const float hr = (float)re, hi = (float)im;
+            if (u.c64) {
+                p[2 * e] = hr;
+                p[2 * e + 1] = hi;
+                continue;
+            }
             p[4 * e] = hr;
             p[4 * e + 1] = hi;
             p[4 * e + 2] = (float)(re - (double)hr);
@@ -733,7 +747,7 @@ void write_umma_pool(const UmmaDesc& u, const GateOp* ops, unsigned char* dst) {
     }
     int pos5[5];
     for (int j = 0; j < 5; ++j) pos5[j] = d.tile_pos[u.tslot[j]];
-    build_umma_gate(ops[u.tc_op], pos5, dst + u.gate_off);
+    build_umma_gate(ops[u.tc_op], pos5, u.c64 != 0, dst + u.gate_off);
 }
 
 std::vector<LaunchPlan> plan_launches(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits, int max_ops,
@@ -753,7 +767,7 @@ std::vector<LaunchPlan> plan_launches(int n, int arith, const std::vector<GateOp
             out.push_back(L);
         }
     };
-    const bool umma = allow_umma && arith == kArithTC && n >= kUmmaTileBits;
+    const bool umma = allow_umma && (arith == kArithTC || arith == kArithTC64) && n >= kUmmaTileBits;
     size_t i = 0;
     while (i < nops) {
         size_t j = i;
@@ -768,15 +782,15 @@ std::vector<LaunchPlan> plan_launches(int n, int arith, const std::vector<GateOp
         // element-wise gates just before the dense gate join its pass
         size_t p = j;
         size_t ewb = 0;
-        while (p > i && elementwise_op(ops[p - 1]) && ewb + ew_pool_bytes(ops[p - 1]) <= kUmmaEwMaxBytes &&
+        while (p > i && elementwise_op(ops[p - 1]) && ewb + ew_pool_bytes(ops[p - 1], arith) <= kUmmaEwMaxBytes &&
                j - p + 1 < (size_t)kMaxOpsPerPass) {
-            ewb += ew_pool_bytes(ops[p - 1]);
+            ewb += ew_pool_bytes(ops[p - 1], arith);
             --p;
         }
         size_t e = j + 1;
-        while (e < nops && elementwise_op(ops[e]) && ewb + ew_pool_bytes(ops[e]) <= kUmmaEwMaxBytes &&
+        while (e < nops && elementwise_op(ops[e]) && ewb + ew_pool_bytes(ops[e], arith) <= kUmmaEwMaxBytes &&
                e - p < (size_t)kMaxOpsPerPass) {
-            ewb += ew_pool_bytes(ops[e]);
+            ewb += ew_pool_bytes(ops[e], arith);
             ++e;
         }
         LaunchPlan L;
@@ -784,7 +798,7 @@ std::vector<LaunchPlan> plan_launches(int n, int arith, const std::vector<GateOp
         int st;
         // leave out gates of the runs until each run's factor depends on at
         // most kUmmaRunBits tile slots
-        while ((st = build_umma(n, ops.data(), p, j, e, L.udesc, by)) == kUmmaPreWide ||
+        while ((st = build_umma(n, arith, ops.data(), p, j, e, L.udesc, by)) == kUmmaPreWide ||
                st == kUmmaPostWide) {
             if (st == kUmmaPreWide) ++p;
             else --e;
@@ -797,7 +811,7 @@ std::vector<LaunchPlan> plan_launches(int n, int arith, const std::vector<GateOp
         classic(i, p);
         L.umma = true;
         L.first = p;
-        L.pool_bytes = L.udesc.gate_off + kUmmaGateBytes;
+        L.pool_bytes = L.udesc.gate_off + (L.udesc.c64 ? kUmmaGateBytes64 : kUmmaGateBytes);
         L.bytes = by;
         out.push_back(L);
         i = e;
@@ -808,7 +822,7 @@ std::vector<LaunchPlan> plan_launches(int n, int arith, const std::vector<GateOp
 uint64_t Workspace::apply_ops(void* state, int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits,
                               int max_ops, uint64_t* passes_out) {
     if (ops.empty()) return 0;
-    if (arith == kArithTC && umma_enabled() && n >= kUmmaTileBits) {
+    if ((arith == kArithTC || arith == kArithTC64) && umma_enabled() && n >= kUmmaTileBits) {
         std::vector<LaunchPlan> L = plan_launches(n, arith, ops, max_tile_bits, max_ops, true);
         size_t total = 0;
         for (auto& l : L) {

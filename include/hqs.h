@@ -45,14 +45,18 @@ extern "C" {
 #define HQS_ARITH_DF 2   /* double-float (2 x FP32), ~48-bit */
 #define HQS_ARITH_F32 3  /* FP32 (complex64 states) */
 #define HQS_ARITH_TC 4   /* complex128: dense 3-5 qubit gates as exact fp16 digit products on the
-                            tensor cores, everything else double-float */
+                            tensor cores (six digits per real; tensor-memory pass from 12 qubits),
+                            everything else double-float */
 #define HQS_ARITH_TF32 5 /* complex64: dense 3-5 qubit gates as 3xTF32 products on the tensor
                             cores (hi*hi + hi*lo + lo*hi, FP32 accumulate), everything else FP32.
-                            The tensor cores' accumulation rounds toward zero: the state's norm
-                            shrinks by about 6.5e-7 per dense 5-qubit gate (measured). */
-#define HQS_ARITH_TC64 6 /* complex64: dense 3-5 qubit gates as exact two-digit fp16 products on
-                            the tensor cores (round to nearest, no norm drift), everything else
-                            FP32. hqs_sim / hqs_server map HQS_ARITH_TC with HQS_C64 to this. */
+                            The tensor cores' accumulation rounds toward zero; each k-step's
+                            products are summed apart and added with round-to-nearest, which
+                            leaves a norm loss of about 7e-8 per dense 5-qubit gate (measured). */
+#define HQS_ARITH_TC64 6 /* complex64: dense 3-5 qubit gates as exact fp16 digit products on the
+                            tensor cores (three digits per real in the tensor-memory pass from
+                            12 qubits, exact levels: no norm drift; two digits below 12 qubits
+                            and in serving batches), everything else FP32. hqs_sim / hqs_server
+                            map HQS_ARITH_TC with HQS_C64 to this. */
 
 typedef struct hqs_sim hqs_sim;
 
@@ -293,9 +297,10 @@ int hqs_plan_passes(int n, int arith, int nops, const int* k, const int* pos, co
                     int max_tile_bits, int max_ops, hqs_pass_info* out, size_t cap, size_t* npasses);
 
 /* The launches hqs_apply_gates makes for the same gates, computed on the host
- * (no GPU): with HQS_ARITH_TC on states of 12 or more qubits, every dense
- * gate on 3-5 qubits gets a tensor-memory pass (tcgen05 tensor cores, TMA tile
- * copies) together with the diagonal / scalar gates around it; the rest are
+ * (no GPU): with HQS_ARITH_TC (complex128) or HQS_ARITH_TC64 (complex64) on
+ * states of 12 or more qubits, every dense gate on 3-5 qubits gets a
+ * tensor-memory pass (tcgen05 tensor cores, TMA tile copies) together with
+ * the diagonal / scalar gates around it; the rest are
  * tiled passes as in hqs_plan_passes. No reference counterpart (the reference
  * runs one sweep per fused gate, SimulatorMPI.cpp:441-541). *nlaunches
  * receives the count; the first cap launches are described in out. */

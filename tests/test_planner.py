@@ -117,7 +117,7 @@ def test_invalid_gates_rejected(hqs):
 
 # ------------------------------------------------------- tensor-memory passes
 
-def _check_umma_launch(n, L, gates):
+def _check_umma_launch(n, L, gates, amp=16):
     tile = L["tile_mask"]
     assert bin(tile).count("1") == 12
     tmask = L["target_mask"]
@@ -149,10 +149,12 @@ def _check_umma_launch(n, L, gates):
         pos += b
     assert pos == n
     assert tbits + L["nextra"] == 12
-    assert L["box_bytes"] == 16 << tbits
+    assert L["box_bytes"] == amp << tbits
+    assert L["sweep_bytes"] == 2 * amp << (n - bin(L["fixed_mask"]).count("1"))
 
 
-def test_umma_launch_plans_cover_gates_and_tile():
+@pytest.mark.parametrize("arith,amp", [("tc", 16), ("tc64", 8)])
+def test_umma_launch_plans_cover_gates_and_tile(arith, amp):
     rng = np.random.default_rng(21)
     for trial in range(60):
         n = int(rng.integers(12, 35))
@@ -166,13 +168,13 @@ def test_umma_launch_plans_cover_gates_and_tile():
                 free = [b for b in range(n) if b not in pos]
                 ctrl = 1 << int(rng.choice(free))
             gates.append((k, pos, ctrl, kind == 0))
-        launches = capi.plan_launches(n, "tc", gates)
+        launches = capi.plan_launches(n, arith, gates)
         nxt = 0
         for L in launches:
             assert L["first_op"] == nxt
             nxt += L["nops"]
             if L["umma"]:
-                _check_umma_launch(n, L, gates)
+                _check_umma_launch(n, L, gates, amp)
                 ops = gates[L["first_op"]:L["first_op"] + L["nops"]]
                 dense = [i for i, g in enumerate(ops) if not g[3] and g[0] >= 3]
                 assert dense == [L["tc_op"]]
@@ -188,5 +190,7 @@ def test_umma_launch_plans_cover_gates_and_tile():
 def test_umma_not_used_below_twelve_qubits_or_other_arithmetic():
     gates = [(5, [0, 2, 4, 6, 8], 0, False)]
     assert not any(L["umma"] for L in capi.plan_launches(11, "tc", gates))
-    assert not any(L["umma"] for L in capi.plan_launches(20, "df", gates))
+    for arith in ("df", "f64", "f32", "tf32"):
+        assert not any(L["umma"] for L in capi.plan_launches(20, arith, gates))
     assert any(L["umma"] for L in capi.plan_launches(20, "tc", gates))
+    assert any(L["umma"] for L in capi.plan_launches(20, "tc64", gates))

@@ -271,3 +271,84 @@ def test_umma_digits_from_double_float():
             err = abs(val - (Fraction(float(hv)) + Fraction(float(lv))))
             worst = max(worst, float(err / Fraction(2) ** (ebf - 126)))
     assert worst < 2.0 ** -46, worst
+
+
+# ---------------------------------------------------------------- complex64
+
+def digits3(x, ef_row):
+    """umma_pass.cu digits3 with the group scale 2^k, k = min(134 - Ef, 126)."""
+    k = min(134 - ef_row, 126)
+    X = F(F(x) * _f32_from_bits((k + 127) << 23))
+    d0 = F(F(X + M0) - M0)
+    r = F(X - d0)
+    d1 = F(F(r * F(512) + M0) - M0)            # the FMA: r * 512 is exact
+    u = F(float(r) * 512.0 - float(d1))        # exact
+    d2 = F(F(u * F(512) + M0) - M0)
+    return [int(d0), int(d1), int(d2)], k
+
+
+def level_sum4_scaled(S, k, ebc):
+    """umma_pass.cu level_sum4, then times the column scale 2^(E_col - 1029)
+    and the group scale 2^-k."""
+    S = [float(F(x)) for x in S]
+    t = F(S[2] * 2.0 ** -18 + float(F(S[3] * 2.0 ** -27)))   # FMA: one rounding
+    v = F(S[0] + float(F(S[1] * 2.0 ** -9 + float(t))))
+    cs = 2.0 ** (ebc - 1029)
+    return F(F(float(v) * cs) * F(2.0 ** -k))
+
+
+def gate_digits3(v, ebmax):
+    """workspace.cpp gate_digits9 with nd = 3."""
+    u = _bits(v)
+    eb = (u >> 52) & 0x7FF
+    a = 0
+    sh = ebmax - eb + 1 + 27
+    if eb and sh < 62:
+        m = (u & ((1 << 52) - 1)) | (1 << 52)
+        a = (m + (1 << (sh - 1)) - 1 + ((m >> sh) & 1)) >> sh
+    r = [a >> 18, (a >> 9) & 511, a & 511]
+    for i in (2, 1):
+        c = (r[i] + 256) >> 9
+        r[i] -= c << 9
+        r[i - 1] += c
+    return [-x if u >> 63 else x for x in r]
+
+
+def test_umma_complex64_digits_levels_and_outputs():
+    """complex64 tensor-memory pass: three state and three gate digits per
+    real, levels 0-3 exact (every level sum below 2^24, also for flat rows
+    against flat columns); the output (level sums by an FMA chain, times the
+    column and group scales)'s error against the exact product of
+    the same float inputs and double gate entries is below 2^-23 of
+    sum_k |x_k b_kn| (the scale an FP32 dot product's own rounding is
+    measured against: a 64-term FP32 sum is accurate to 64 2^-24 of it in
+    the worst case)."""
+    rng = np.random.default_rng(23)
+    h5 = np.array([[(-1) ** bin(r & c).count("1") for c in range(32)] for r in range(32)]) / math.sqrt(32.0)
+    worst = 0.0
+    cases = []
+    for trial in range(4):
+        q, _ = np.linalg.qr(rng.standard_normal((32, 32)) + 1j * rng.standard_normal((32, 32)))
+        x = (rng.standard_normal(64) * np.exp(rng.uniform(-8, 0, 64)) * 2.0 ** -int(rng.integers(0, 20))).astype(np.float32)
+        cases.append((real_form(q), x))
+    cases.append((real_form(h5.astype(np.complex128)), np.full(64, 1 / 8.0, dtype=np.float32)))
+    for b, x in cases:
+        ef = max((_f32_bits(v) >> 23) & 0xFF for v in x)
+        dx = [digits3(v, ef)[0] for v in x]
+        k = digits3(x[0], ef)[1]
+        assert all(abs(d) <= 256 for dd in dx for d in dd)
+        for n in range(0, 64, 5):
+            ebc = max((_bits(b[k, n]) >> 52) & 0x7FF for k in range(64))
+            de = [gate_digits3(b[k, n], ebc) for k in range(64)]
+            assert all(abs(e[0]) <= 128 and abs(e[1]) <= 256 and abs(e[2]) <= 256 for e in de)
+            S = [0] * 4
+            for i in range(3):
+                for j in range(3):
+                    if i + j <= 3:
+                        S[i + j] += sum(dx[k][i] * de[k][j] for k in range(64))
+            assert all(abs(v) < 1 << 24 for v in S), S
+            y = level_sum4_scaled(S, k, ebc)
+            exact = sum(Fraction(float(x[k])) * Fraction(b[k, n]) for k in range(64))
+            scale = sum(abs(float(x[k]) * b[k, n]) for k in range(64))
+            worst = max(worst, abs(float(Fraction(float(y)) - exact)) / scale)
+    assert worst < 2.0 ** -23, worst
