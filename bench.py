@@ -542,9 +542,10 @@ def parity_headline(args, cmds, zz, shots):
                           "layout_changed": pmap != gmap,
                           "amplitudes_max_abs_vs_oracle": max_abs_diff(pvec, pmap, rvec, rmap, n)}
     del pvec, before
-    zg = [sim.get_expectation_value([([(a, "Z"), (b, "Z")], 1.0)], ids) for a, b in zz]
+    zg = sim.get_expectation_values([[([(a, "Z"), (b, "Z")], 1.0)] for a, b in zz], ids)
     zr = [ref.get_expectation_value([([(a, "Z"), (b, "Z")], 1.0)], ids) for a, b in zz]
-    out["zz"] = {"pairs": len(zz), "max_abs": float(np.max(np.abs(np.array(zg) - np.array(zr))))}
+    out["zz"] = {"pairs": len(zz), "max_abs": float(np.max(np.abs(np.array(zg) - np.array(zr)))),
+                 "call": "get_expectation_values (the 64 pairs in one read of the state)"}
     out["norm_minus_1"] = sim.get_probability([], []) - 1.0
     out["pass"] = bool(out["amplitudes_max_abs"] <= 1e-12 and out["permutation"]["bit_exact"]
                        and out["permutation"]["amplitudes_max_abs_vs_oracle"] <= 1e-12
@@ -603,8 +604,8 @@ def run_tour(args):
     args.qubits-qubit state (the workload for the per-kernel ncu summaries):
     fused passes of the benchmark circuit in tensor-core digit mode and in
     double-float mode, probability, the measurement block sums, Z-string and
-    general Pauli expectation values, the qubit permutation, collapse, the
-    drop of a qubit and one batched serving round."""
+    general Pauli expectation values, 64 <Z_a Z_b> in one call, the qubit
+    permutation, collapse, the drop of a qubit and one batched serving run."""
     import hiqsimulator_gb300 as hqs
     from hiqsimulator_gb300 import circuits, serving
     n = N_QUBITS
@@ -634,13 +635,15 @@ def run_tour(args):
     smp = sim.sample(64)
     zz = sim.get_expectation_value([([(2, "Z"), (n - 1, "Z")], 1.0)], ids)
     xy = sim.get_expectation_value([([(0, "X"), (5, "Y")], 0.5), ([(7, "Z")], 0.25)], ids)
+    zz64 = sim.get_expectation_values([[([(a, "Z"), (b, "Z")], 1.0)] for a, b in circuits.zz_pairs_and_shots(SEED, n)[0]],
+                                      ids)
     force_permutation(sim)
     low = sim.get_qubits_ids()[0]  # the qubit now at position 0: dropping it compacts the whole state
     p0 = sim.get_probability([True], [low])
     sim.collapse_wavefunction([low], [p0 > 0.5])
     sim.deallocate_qubit(low)
     sim.synchronize()
-    log("tour queries: p %.3f, %d samples, zz %.3e, xy %.3e" % (p, len(smp), zz, xy))
+    log("tour queries: p %.3f, %d samples, zz %.3e, xy %.3e, 64 zz sum %.3e" % (p, len(smp), zz, xy, sum(zz64)))
     del sim
     work = serving.serving_workload(11, 24)
     res, st = serving.serve(work, np.zeros(len(work)), precision="c128", arith="tc", budget_bytes=8e9, max_active=24)
@@ -775,7 +778,7 @@ def run_ours(args, dist):
         circuits.replay(s, cmds)
         s.run()
         force_permutation(s)
-        ev = [s.get_expectation_value([([(a, "Z"), (b, "Z")], 1.0)], ids) for a, b in zz]
+        ev = s.get_expectation_values([[([(a, "Z"), (b, "Z")], 1.0)] for a, b in zz], ids)
         smp = s.sample(shots)
         return ev, smp
 

@@ -275,6 +275,23 @@ int hqs_sim_get_expectation_value(hqs_sim* sim, size_t nterms, const size_t* ter
     });
 }
 
+int hqs_sim_get_expectation_values(hqs_sim* sim, size_t nops, const size_t* op_off, const size_t* term_off,
+                                   const int64_t* factor_index, const char* factor_pauli, const double* coefs,
+                                   const int64_t* ids, size_t nids, double* out) {
+    SIM_CALL(sim, {
+        need(nops == 0 || (op_off && out), "null arrays");
+        need(nids == 0 || ids, "null ids");
+        if (nops == 0) return;
+        need(op_off[0] == 0, "operator offsets must start at 0");
+        for (size_t o = 0; o < nops; ++o) need(op_off[o] <= op_off[o + 1], "operator offsets must not decrease");
+        const auto terms = decode_terms(op_off[nops], term_off, factor_index, factor_pauli, coefs);
+        std::vector<std::vector<hqs::PauliTerm>> ops(nops);
+        for (size_t o = 0; o < nops; ++o) ops[o].assign(terms.begin() + op_off[o], terms.begin() + op_off[o + 1]);
+        const std::vector<double> v = sim->eng->get_expectation_values(ops, std::vector<int64_t>(ids, ids + nids));
+        std::copy(v.begin(), v.end(), out);
+    });
+}
+
 int hqs_sim_apply_qubit_operator(hqs_sim* sim, size_t nterms, const size_t* term_off, const int64_t* factor_index,
                                  const char* factor_pauli, const double* coefs, const int64_t* ids, size_t nids) {
     SIM_CALL(sim, {

@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <numeric>
 
 namespace hqs {
@@ -519,6 +520,47 @@ double Engine::get_expectation_value(const std::vector<PauliTerm>& terms, const 
                                         (const uint64_t*)(d + 2 * T * 8), (const double*)(d + 3 * T * 8), ws_.reduce(),
                                         ws_.stream(), &out),
                "reduce_pauli_expectation");
+    return out;
+}
+
+std::vector<double> Engine::get_expectation_values(const std::vector<std::vector<PauliTerm>>& ops,
+                                                   const std::vector<int64_t>& ids) {
+    run();
+    flush();
+    std::vector<double> out(ops.size(), 0.0);
+    std::vector<uint64_t> masks;  // distinct Z strings of the Z-only operators
+    std::map<uint64_t, size_t> slot;
+    std::vector<std::vector<uint64_t>> zterms(ops.size());
+    std::vector<char> zonly(ops.size(), 0);
+    for (size_t o = 0; o < ops.size(); ++o) {
+        std::vector<uint64_t> xm, ym, zm;
+        pauli_masks(ops[o], ids, xm, ym, zm);
+        bool z = true;
+        for (uint64_t x : xm) z = z && x == 0;
+        if (!z) {
+            out[o] = get_expectation_value(ops[o], ids);
+            continue;
+        }
+        zonly[o] = 1;
+        zterms[o] = zm;
+        for (uint64_t m : zm)
+            if (slot.emplace(m, masks.size()).second) masks.push_back(m);
+    }
+    // <Z string> = sum_i (-1)^popcount(i & z) |a_i|^2 (real); Re(c <P>) = Re(c) <P>
+    std::vector<double> val(masks.size(), 0.0);
+    for (size_t b = 0; b < masks.size(); b += 64) {
+        const int T = (int)std::min<size_t>(64, masks.size() - b);
+        const uint64_t* d_z = static_cast<const uint64_t*>(ws_.upload(masks.data() + b, (size_t)T * 8));
+        double* scratch = static_cast<double*>(ws_.scratch(zparity_multi_scratch_bytes(T)));
+        cuda_check(reduce_zparity_multi(arith_, state_, n(), T, d_z, scratch, ws_.stream(), val.data() + b),
+                   "reduce_zparity_multi");
+    }
+    for (size_t o = 0; o < ops.size(); ++o) {
+        if (!zonly[o]) continue;
+        double v = 0.0;
+        for (size_t t = 0; t < ops[o].size(); ++t) v += ops[o][t].coef.real() * val[slot[zterms[o][t]]];
+        out[o] = v;
+    }
     return out;
 }
 

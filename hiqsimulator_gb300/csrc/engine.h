@@ -70,6 +70,11 @@ public:
     void cheat_local(cplx* out, size_t cap);
     // --- methods the Python backend calls that the reference never bound ---
     double get_expectation_value(const std::vector<PauliTerm>& terms, const std::vector<int64_t>& ids);
+    // One value per operator (extension): the distinct Z strings of the
+    // operators made only of Z strings share one read of the state per 64;
+    // the other operators go through get_expectation_value.
+    std::vector<double> get_expectation_values(const std::vector<std::vector<PauliTerm>>& ops,
+                                               const std::vector<int64_t>& ids);
     void apply_qubit_operator(const std::vector<PauliTerm>& terms, const std::vector<int64_t>& ids);
     void set_wavefunction(const cplx* wf, size_t len, const std::vector<int64_t>& ids);
 

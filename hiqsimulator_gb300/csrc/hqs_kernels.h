@@ -65,6 +65,12 @@ cudaError_t block_sums(int arith, const void* state, int n, uint64_t nblocks, do
 // Pauli-sum expectation: sum_t Re(c_t <psi|P_t|psi>); masks/coefs in device memory.
 // With zonly (one term, no X or Y) the device masks are not read: out is the
 // signed norm sum_i (-1)^popcount(i & zmask0) |a_i|^2, to be scaled by Re(c).
+// E[t] = sum_i (-1)^popcount(i & z[t]) |a_i|^2 for T <= 64 masks (device
+// array d_z) in one read of the state; d_scratch holds
+// zparity_multi_scratch_bytes(T); out (host, T doubles) receives E. Synchronizes s.
+cudaError_t reduce_zparity_multi(int arith, const void* state, int n, int T, const uint64_t* d_z, double* d_scratch,
+                                 cudaStream_t s, double* out);
+size_t zparity_multi_scratch_bytes(int T);
 cudaError_t reduce_pauli_expectation(int arith, const void* state, int n, int nterms, const uint64_t* d_xm,
                                      const uint64_t* d_ym, const uint64_t* d_zm, const double* d_coef,
                                      ReduceScratch& rs, cudaStream_t s, double* out, bool zonly = false,

@@ -1163,6 +1163,102 @@ __global__ void __launch_bounds__(kThreads) zparity_kernel(const S* __restrict__
     if (threadIdx.x == 0) partials[blockIdx.x] = v[0];
 }
 
+// ---- many Z strings in one read of the state
+// E_t = sum_i (-1)^popcount(i & z_t) |a_i|^2 for up to kZMulti masks. The
+// state is taken in chunks of 2^q consecutive amplitudes (q = min(n, 12));
+// per chunk c the Walsh coefficients W_c[m] = sum_lo (-1)^popcount(lo & m)
+// |a_(c 2^q + lo)|^2 of all 2^q low masks come from a fast Walsh-Hadamard
+// transform in double-float (16 elements per thread: the four stages over
+// index bits 8-11 in registers, the others in shared memory), and mask t
+// adds (-1)^popcount(c 2^q & z_t) W_c[z_t mod 2^q]. Cost per amplitude: one
+// load and q double-float butterflies, whatever the number of masks.
+constexpr int kZMulti = 64;
+
+// (a, b) <- (a + b, a - b) in double-float
+__device__ __forceinline__ void df_butterfly(float& ah, float& al, float& bh, float& bl) {
+    const float sh = ah + bh, sv = sh - ah;
+    const float se = (ah - (sh - sv)) + (bh - sv) + al + bl;
+    const float dh = ah - bh, dv = dh - ah;
+    const float de = (ah - (dh - dv)) + (-bh - dv) + al - bl;
+    const float s2 = sh + se, d2 = dh + de;
+    ah = s2;
+    al = se - (s2 - sh);
+    bh = d2;
+    bl = de - (d2 - dh);
+}
+
+template <class S>
+__global__ void __launch_bounds__(kThreads, 4) zparity_multi_kernel(const S* __restrict__ state, int n, int T,
+                                                                 const uint64_t* __restrict__ z,
+                                                                 double* __restrict__ partials) {
+    __shared__ float wh[4096], wl[4096];
+    const int q = n < 12 ? n : 12;
+    const uint32_t Q = 1u << q;
+    const uint64_t nchunks = 1ULL << (n - q);
+    const uint64_t zt = (int)threadIdx.x < T ? z[threadIdx.x] : 0;
+    float ah = 0.f, al = 0.f;  // mask threadIdx.x's sum (threads < T)
+    for (uint64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+        const S* base = state + (c << q);
+        if (q == 12) {
+            // element tid + 256 j: j holds index bits 8-11
+            float vh[16], vl[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const S a = base[threadIdx.x + 256 * j];
+                norm2_df(a, vh[j], vl[j]);
+            }
+#pragma unroll
+            for (int b = 0; b < 4; ++b)
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    if (!((j >> b) & 1)) df_butterfly(vh[j], vl[j], vh[j | (1 << b)], vl[j | (1 << b)]);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                wh[threadIdx.x + 256 * j] = vh[j];
+                wl[threadIdx.x + 256 * j] = vl[j];
+            }
+        } else {
+            for (uint32_t i = threadIdx.x; i < Q; i += kThreads) norm2_df(base[i], wh[i], wl[i]);
+        }
+        __syncthreads();
+        for (int b = 0; b < (q == 12 ? 8 : q); ++b) {
+            for (uint32_t k = threadIdx.x; k < Q / 2; k += kThreads) {
+                const uint32_t i = ((k >> b) << (b + 1)) | (k & ((1u << b) - 1u));
+                const uint32_t j = i | (1u << b);
+                float xh = wh[i], xl = wl[i], yh = wh[j], yl = wl[j];
+                df_butterfly(xh, xl, yh, yl);
+                wh[i] = xh;
+                wl[i] = xl;
+                wh[j] = yh;
+                wl[j] = yl;
+            }
+            __syncthreads();
+        }
+        if ((int)threadIdx.x < T) {
+            const uint32_t m = (uint32_t)(zt & (Q - 1u));
+            float vh = wh[m], vl = wl[m];
+            if (__popcll((c << q) & zt) & 1) {
+                vh = -vh;
+                vl = -vl;
+            }
+            const float s2 = ah + vh, bb = s2 - ah;
+            al += ((ah - (s2 - bb)) + (vh - bb)) + vl;
+            ah = s2;
+        }
+        __syncthreads();
+    }
+    if ((int)threadIdx.x < T) partials[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = (double)ah + (double)al;
+}
+
+// out[t] = the fixed-order FP64 sum of mask t's per-CTA partials
+__global__ void finish_multi_kernel(const double* __restrict__ partials, int nparts, double* __restrict__ out) {
+    __shared__ double red[32];
+    double v[1] = {0.0};
+    for (int p = threadIdx.x; p < nparts; p += blockDim.x) v[0] += partials[(size_t)blockIdx.x * nparts + p];
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) out[blockIdx.x] = v[0];
+}
+
 // One term of a Pauli sum as the expectation kernel uses it: x the flip
 // mask, yz the sign mask, h the lowest bit of x (an unordered pair {i, i^x}
 // is visited from its member with bit h clear), im whether the pair
@@ -1555,6 +1651,33 @@ cudaError_t block_sums(int arith, const void* state, int n, uint64_t nblocks, do
             block_sum_serial_kernel<NormAccDF, float2><<<g, kThreads, 0, s>>>((const float2*)state, K, nblocks, d_out);
     }
     return cudaGetLastError();
+}
+
+cudaError_t reduce_zparity_multi(int arith, const void* state, int n, int T, const uint64_t* d_z, double* d_scratch,
+                                 cudaStream_t s, double* out) {
+    arith = base_arith(arith);
+    if (T < 1 || T > kZMulti) return cudaErrorInvalidValue;
+    const int q = n < 12 ? n : 12;
+    const uint64_t nchunks = 1ULL << (n - q);
+    const int g = (int)std::min<uint64_t>(nchunks, (uint64_t)device_sm_count() * 4);
+    double* partials = d_scratch;
+    double* d_out = d_scratch + (size_t)T * g;
+    if (arith == kArithF32)
+        zparity_multi_kernel<float2><<<g, kThreads, 0, s>>>((const float2*)state, n, T, d_z, partials);
+    else
+        zparity_multi_kernel<double2><<<g, kThreads, 0, s>>>((const double2*)state, n, T, d_z, partials);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    finish_multi_kernel<<<T, kThreads, 0, s>>>(partials, g, d_out);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpyAsync(out, d_out, (size_t)T * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+    return cudaStreamSynchronize(s);
+}
+
+size_t zparity_multi_scratch_bytes(int T) {
+    return sizeof(double) * ((size_t)T * (size_t)device_sm_count() * 4 + (size_t)T);
 }
 
 cudaError_t reduce_pauli_expectation(int arith, const void* state, int n, int nterms, const uint64_t* d_xm,

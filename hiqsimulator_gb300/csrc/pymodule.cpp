@@ -246,6 +246,24 @@ public:
                                             a.coefs.data(), ids.data(), ids.size(), &out));
         return out;
     }
+    // one value per operator; Z-only operators share one read of the state per 64 Z strings
+    std::vector<double> get_expectation_values(const py::object& ops, const Ids& ids) {
+        PauliArgs all;
+        std::vector<size_t> op_off{0};
+        for (py::handle op : ops) {
+            const PauliArgs a = encode(py::reinterpret_borrow<py::object>(op));
+            const size_t base = all.idx.size();
+            for (size_t t = 1; t < a.off.size(); ++t) all.off.push_back(base + a.off[t]);
+            all.idx.insert(all.idx.end(), a.idx.begin(), a.idx.end());
+            all.pauli.insert(all.pauli.end(), a.pauli.begin(), a.pauli.end());
+            all.coefs.insert(all.coefs.end(), a.coefs.begin(), a.coefs.end());
+            op_off.push_back(all.off.size() - 1);
+        }
+        std::vector<double> out(op_off.size() - 1, 0.0);
+        check(hqs_sim_get_expectation_values(h_, out.size(), op_off.data(), all.off.data(), all.idx.data(),
+                                             all.pauli.data(), all.coefs.data(), ids.data(), ids.size(), out.data()));
+        return out;
+    }
     void apply_qubit_operator(const py::object& op, const Ids& ids) {
         const PauliArgs a = encode(op);
         check(hqs_sim_apply_qubit_operator(h_, a.off.size() - 1, a.off.data(), a.idx.data(), a.pauli.data(),
@@ -377,6 +395,7 @@ PYBIND11_MODULE(_cppsim_mpi, m) {
         .def("collapse_wavefunction", &SimulatorMPI::collapse_wavefunction)
         .def("get_expectation_value", &SimulatorMPI::get_expectation_value)
         .def("apply_qubit_operator", &SimulatorMPI::apply_qubit_operator)
+        .def("get_expectation_values", &SimulatorMPI::get_expectation_values)
         .def("set_wavefunction", &SimulatorMPI::set_wavefunction)
         .def("emulate_time_evolution", &SimulatorMPI::emulate_time_evolution)
         .def("cheat_local_numpy", &SimulatorMPI::cheat_local_numpy)

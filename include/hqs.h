@@ -132,6 +132,16 @@ int hqs_sim_emulate_math(hqs_sim* sim);
 int hqs_sim_get_expectation_value(hqs_sim* sim, size_t nterms, const size_t* term_off, const int64_t* factor_index,
                                   const char* factor_pauli, const double* coefs, const int64_t* ids, size_t nids,
                                   double* out);
+/* Several expectation values in one call (extension; no reference
+ * counterpart): operator o is the terms [op_off[o], op_off[o + 1]) of the
+ * term arrays laid out as for hqs_sim_get_expectation_value (term t has
+ * factors [term_off[t], term_off[t + 1]) and coefficient coefs[2t] + i
+ * coefs[2t + 1]); out[o] receives its value. The distinct Z strings of the
+ * operators made only of Z factors share one read of the state per 64
+ * strings; other operators take one hqs_sim_get_expectation_value each. */
+int hqs_sim_get_expectation_values(hqs_sim* sim, size_t nops, const size_t* op_off, const size_t* term_off,
+                                   const int64_t* factor_index, const char* factor_pauli, const double* coefs,
+                                   const int64_t* ids, size_t nids, double* out);
 int hqs_sim_apply_qubit_operator(hqs_sim* sim, size_t nterms, const size_t* term_off, const int64_t* factor_index,
                                  const char* factor_pauli, const double* coefs, const int64_t* ids, size_t nids);
 /* set_wavefunction(wf, ids): called at _simulator_mpi.py:305-306. wf: len

@@ -253,6 +253,52 @@ def test_pauli_sums_match_oracle(hqs, cuda, prec):
     assert abs(sim.get_expectation_value(op, ids) - want) < tol
 
 
+@pytest.mark.parametrize("n,prec", [(14, "c128"), (9, "c128"), (13, "c64")])
+def test_get_expectation_values_matches_oracle(hqs, cuda, n, prec):
+    """The batched extension: 64 <Z_a Z_b> pairs, Z-only sums with complex
+    coefficients and the empty string, operators with X/Y factors (the
+    general path), more than 64 distinct Z strings (two reads of the state),
+    before and after a qubit permutation; states of fewer than 12 qubits
+    (one transform chunk) too."""
+    from oracle.engine import OracleSimulator
+    rng = np.random.Generator(np.random.PCG64(41 + n))
+    ids = list(range(n))
+    psi = rng.standard_normal(1 << n) + 1j * rng.standard_normal(1 << n)
+    psi /= np.linalg.norm(psi)
+    if prec == "c64":
+        psi = psi.astype(np.complex64).astype(np.complex128)
+    ops = []
+    for _ in range(64):
+        a, b = rng.choice(n, size=2, replace=False)
+        ops.append([([(int(a), "Z"), (int(b), "Z")], 1.0)])
+    for _ in range(30):
+        terms = []
+        for t in range(int(rng.integers(1, 5))):
+            w = int(rng.integers(0, 4))
+            qs = sorted(int(q) for q in rng.choice(n, size=w, replace=False))
+            terms.append(([(q, "Z") for q in qs], complex(rng.standard_normal(), rng.standard_normal())))
+        ops.append(terms)
+    ops.append([([(0, "X"), (n - 1, "Y")], 0.5), ([(2, "Z")], 1.5)])
+    ops.append([])
+    sim = hqs.SimulatorMPI(5, 20, 4, prec)
+    ref = OracleSimulator(5, 20, 4)
+    for s_ in (sim, ref):
+        s_.allocate_qureg(ids, 0)
+        s_.set_wavefunction(psi.tolist(), ids)
+    tol = 1e-11 if prec == "c128" else 2e-6
+    want = [ref.get_expectation_value(op, ids) if op else 0.0 for op in ops]
+    got = sim.get_expectation_values(ops, ids)
+    assert len(got) == len(ops)
+    assert np.max(np.abs(np.array(got) - want)) < tol
+    single = [sim.get_expectation_value(op, ids) for op in ops[:70]]
+    assert np.max(np.abs(np.array(single) - got[:70])) < tol
+    sim.move_qubits([n - 1, n - 2, n - 3], [0, 1, 2])
+    got2 = sim.get_expectation_values(ops, ids)
+    assert np.max(np.abs(np.array(got2) - want)) < tol
+    with pytest.raises(RuntimeError):
+        sim.get_expectation_values([[([(n + 3, "Z")], 1.0)]], ids)
+
+
 def test_apply_qubit_operator_known_answers(make):
     """Commented-out reference test _simulator_mpi_test.py:454-478."""
     sim = make()
