@@ -11,6 +11,7 @@ import numpy as np
 
 from .lib import MT19937, dptr, load_oracle_lib
 import ctypes
+import time
 
 
 class Fusion:
@@ -185,6 +186,11 @@ class OracleSimulator:
 
     def run(self):
         """SimulatorMPI.cpp:441-541."""
+        self.run_timed()
+
+    def run_timed(self):
+        """run(), returning the seconds spent in the state sweep alone (the
+        fusion of the queued gates is not timed)."""
         M, ids, ctrls, diag = self.fusion.perform_fusion()
         ctrl_mask = 0
         for c in ctrls:
@@ -195,8 +201,11 @@ class OracleSimulator:
         if k > 5:
             # the reference throws before resetting its fusion queue
             raise RuntimeError("Run(): cannot apply %d qubits gate" % k)
+        t0 = time.perf_counter()
         self.apply_matrix(M, pos, ctrl_mask, diag)
+        dt = time.perf_counter() - t0
         self.fusion = Fusion()
+        return dt
 
     def apply_matrix(self, M, pos, ctrl_mask=0, diag=False):
         M = np.ascontiguousarray(M, dtype=np.complex128)
