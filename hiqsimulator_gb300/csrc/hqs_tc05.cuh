@@ -95,6 +95,32 @@ __device__ __forceinline__ void tmem_ld8(uint32_t ta, uint32_t (&r)[8]) {
                  : "r"(ta));
 }
 __device__ __forceinline__ void tmem_ld_wait() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tmem_ld4(uint32_t ta, uint32_t (&r)[4]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0,%1,%2,%3}, [%4];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(ta));
+}
+// tcgen05.wait::ld for loads whose registers are still to be used: the
+// registers pass through the asm, so no use of them is scheduled before the
+// wait (the loads of the next chunk may be in flight while the current one
+// is processed)
+__device__ __forceinline__ void tmem_ld_wait_regs(uint32_t (&r)[6][4]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0][0]), "+r"(r[0][1]), "+r"(r[0][2]), "+r"(r[0][3]), "+r"(r[1][0]), "+r"(r[1][1]),
+                   "+r"(r[1][2]), "+r"(r[1][3]), "+r"(r[2][0]), "+r"(r[2][1]), "+r"(r[2][2]), "+r"(r[2][3]),
+                   "+r"(r[3][0]), "+r"(r[3][1]), "+r"(r[3][2]), "+r"(r[3][3]), "+r"(r[4][0]), "+r"(r[4][1]),
+                   "+r"(r[4][2]), "+r"(r[4][3]), "+r"(r[5][0]), "+r"(r[5][1]), "+r"(r[5][2]), "+r"(r[5][3])
+                 :
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld_wait_regs(uint32_t (&r)[4][4]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0][0]), "+r"(r[0][1]), "+r"(r[0][2]), "+r"(r[0][3]), "+r"(r[1][0]), "+r"(r[1][1]),
+                   "+r"(r[1][2]), "+r"(r[1][3]), "+r"(r[2][0]), "+r"(r[2][1]), "+r"(r[2][2]), "+r"(r[2][3]),
+                   "+r"(r[3][0]), "+r"(r[3][1]), "+r"(r[3][2]), "+r"(r[3][3])
+                 :
+                 : "memory");
+}
 __device__ __forceinline__ void tmem_st8(uint32_t ta, const uint32_t (&r)[8]) {
     asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(ta), "r"(r[0]),
                  "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7])

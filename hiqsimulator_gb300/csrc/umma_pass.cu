@@ -717,15 +717,22 @@ __global__ void __launch_bounds__(kThreadsU, 1)
                 // tensor-memory loads are warp-collective: every thread takes
                 // part, also for a group that keeps its inputs.
                 const int Eb = erow[g];
+                // four chunks of four output reals; the next chunk's loads are
+                // in flight while the current one is assembled
+                uint32_t r[4][6][4];
 #pragma unroll
-                for (int ch = 0; ch < 2; ++ch) {
-                    const uint32_t n0 = (uint32_t)(part * 16 + ch * 8);
-                    uint32_t r[6][8];
+                for (int lev = 0; lev < 6; ++lev) tmem_ld4(tmem + lane_base + (uint32_t)lev * 64u + (uint32_t)(part * 16), r[0][lev]);
+                tmem_ld_wait_regs(r[0]);
 #pragma unroll
-                    for (int lev = 0; lev < 6; ++lev) tmem_ld8(tmem + lane_base + (uint32_t)lev * 64u + n0, r[lev]);
-                    tmem_ld_wait();
+                for (int ch = 0; ch < 4; ++ch) {
+                    const uint32_t n0 = (uint32_t)(part * 16 + ch * 4);
+                    if (ch < 3) {
 #pragma unroll
-                    for (int a = 0; a < 4; ++a) {
+                        for (int lev = 0; lev < 6; ++lev)
+                            tmem_ld4(tmem + lane_base + (uint32_t)lev * 64u + n0 + 4u, r[ch + 1][lev]);
+                    }
+#pragma unroll
+                    for (int a = 0; a < 2; ++a) {
                         const uint32_t L = gbase | offt[(n0 >> 1) + a];
                         if (!write) {  // the pre-run was stored with the digits
                             if (post)
@@ -737,9 +744,9 @@ __global__ void __launch_bounds__(kThreadsU, 1)
 #pragma unroll
                         for (int p = 0; p < 2; ++p) {
                             const int c = a * 2 + p;
-                            const float S[6] = {__uint_as_float(r[0][c]), __uint_as_float(r[1][c]),
-                                                __uint_as_float(r[2][c]), __uint_as_float(r[3][c]),
-                                                __uint_as_float(r[4][c]), __uint_as_float(r[5][c])};
+                            const float S[6] = {__uint_as_float(r[ch][0][c]), __uint_as_float(r[ch][1][c]),
+                                                __uint_as_float(r[ch][2][c]), __uint_as_float(r[ch][3][c]),
+                                                __uint_as_float(r[ch][4][c]), __uint_as_float(r[ch][5][c])};
                             level_sum_to_df(S, h[p], l[p]);
                         }
                         if (post) {
@@ -754,6 +761,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
                                          : make_double2(df_to_double_scaled(h[0], l[0], Eb + ecol[n0 + c0] - 2059),
                                                         df_to_double_scaled(h[1], l[1], Eb + ecol[n0 + c0 + 1] - 2059));
                     }
+                    if (ch < 3) tmem_ld_wait_regs(r[ch + 1]);
                 }
             } else if (post) {
                 run_apply(buf, tab_post, lut_post);
@@ -855,15 +863,20 @@ __global__ void __launch_bounds__(kThreadsU, 1)
                 const int gexp = erow[g];
                 const float gs = __uint_as_float((uint32_t)gexp << 23);  // 0 for a zero group
                 const float* cs = reinterpret_cast<const float*>(sm + S::kEcol);
+                uint32_t r[4][4][4];
 #pragma unroll
-                for (int ch = 0; ch < 2; ++ch) {
-                    const uint32_t n0 = (uint32_t)(part * 16 + ch * 8);
-                    uint32_t r[4][8];
+                for (int lev = 0; lev < 4; ++lev) tmem_ld4(tmem + lane_base + (uint32_t)lev * 64u + (uint32_t)(part * 16), r[0][lev]);
+                tmem_ld_wait_regs(r[0]);
 #pragma unroll
-                    for (int lev = 0; lev < 4; ++lev) tmem_ld8(tmem + lane_base + (uint32_t)lev * 64u + n0, r[lev]);
-                    tmem_ld_wait();
+                for (int ch = 0; ch < 4; ++ch) {
+                    const uint32_t n0 = (uint32_t)(part * 16 + ch * 4);
+                    if (ch < 3) {
 #pragma unroll
-                    for (int a = 0; a < 4; ++a) {
+                        for (int lev = 0; lev < 4; ++lev)
+                            tmem_ld4(tmem + lane_base + (uint32_t)lev * 64u + n0 + 4u, r[ch + 1][lev]);
+                    }
+#pragma unroll
+                    for (int a = 0; a < 2; ++a) {
                         const uint32_t L = gbase | offt[(n0 >> 1) + a];
                         if (!write) {  // the pre-run was stored with the digits
                             if (post) buf[L] = ArithF32::mul(tab_post[run_index(lut_post, L)], buf[L]);
@@ -873,16 +886,17 @@ __global__ void __launch_bounds__(kThreadsU, 1)
 #pragma unroll
                         for (int p = 0; p < 2; ++p) {
                             const int c = a * 2 + p;
-                            const float Sl[4] = {__uint_as_float(r[0][c]), __uint_as_float(r[1][c]),
-                                                 __uint_as_float(r[2][c]), __uint_as_float(r[3][c])};
+                            const float Sl[4] = {__uint_as_float(r[ch][0][c]), __uint_as_float(r[ch][1][c]),
+                                                 __uint_as_float(r[ch][2][c]), __uint_as_float(r[ch][3][c])};
                             y[p] = __fmul_rn(__fmul_rn(level_sum4(Sl), cs[n0 + c]), gs);
                         }
                         float2 v = make_float2(y[0], y[1]);
                         if (post) v = ArithF32::mul(tab_post[run_index(lut_post, L)], v);
                         buf[L] = v;
                     }
+                    if (ch < 3) tmem_ld_wait_regs(r[ch + 1]);
                 }
-            } else if (post) {
+                        } else if (post) {
                 run_apply64(buf, tab_post, lut_post);
             }
             fence_proxy_async();
