@@ -621,7 +621,7 @@ def run_tour(args):
     """One launch or a few of every state-streaming kernel on an
     args.qubits-qubit state (the workload for the per-kernel ncu summaries):
     fused passes of the benchmark circuit in tensor-core digit mode and in
-    double-float mode, probability, the measurement block sums, Z-string and
+    double-float mode (complex128) and in the complex64 tensor-core mode, probability, the measurement block sums, Z-string and
     general Pauli expectation values, 64 <Z_a Z_b> in one call, the qubit
     permutation, collapse, the drop of a qubit and one batched serving run."""
     import hiqsimulator_gb300 as hqs
@@ -648,6 +648,16 @@ def run_tour(args):
 
     sim = replayed("df")
     del sim
+    # the complex64 tensor-memory pass on the last 24 fused gates (random layers: dense gates alone)
+    run_at = [i for i, c in enumerate(cmds) if c[0] == "run"]
+    tail = cmds[run_at[-25] + 1:] if len(run_at) > 25 else cmds
+    c64 = hqs.SimulatorMPI(SEED, n, CLUSTER, "c64", "tc")
+    c64.allocate_qureg(ids, 0)
+    circuits.replay(c64, tail)
+    c64.run()
+    c64.synchronize()
+    log("tour c64: %d fused gates" % runs)
+    del c64
     sim = replayed("tc")
     p = sim.get_probability([True], [3])
     smp = sim.sample(64)

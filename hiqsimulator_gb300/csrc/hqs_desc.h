@@ -82,7 +82,7 @@ constexpr int kUmmaGroups = 128;
 constexpr int kUmmaDigits = 6;
 constexpr uint32_t kUmmaGatePlaneBytes = 6 * 64 * 128;           // six gate digit planes, 64 rows x 128 B
 constexpr uint32_t kUmmaGateBytes = kUmmaGatePlaneBytes + 64 * 4;  // + column exponents
-// complex64: three gate digit planes and a zero plane, then the column exponents
+// complex64: four gate digit planes, then the column exponents
 constexpr uint32_t kUmmaGatePlaneBytes64 = 4 * 64 * 128;
 constexpr uint32_t kUmmaGateBytes64 = kUmmaGatePlaneBytes64 + 64 * 4;
 constexpr uint32_t kUmmaEwMaxBytes = 13 * 512;                     // element-wise matrices staged per pass
@@ -97,7 +97,7 @@ struct UmmaDesc {
     uint8_t tslot[5];      // tile slots of the five targets, ascending (element bits 0..4)
     uint8_t rank;          // tensor-map rank (1..5)
     uint8_t nextra;        // tile bits above the box (one copy per combination)
-    uint8_t c64;           // 1: complex64 state (three digits per real), 0: complex128
+    uint8_t c64;           // 1: complex64 state (three digits per state real, four per gate real), 0: complex128
     int8_t dim_kind[5];    // 1: a run of tile positions (the box) and the gap above it (coordinate
                            // from the tile base); 2: the same, last, with the extra tile bits above
                            // its run (coordinate from the tile base plus the copy's extra bits)

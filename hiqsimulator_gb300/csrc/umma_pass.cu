@@ -4,8 +4,8 @@
 // sweep over the state. Replaces, for its pass, the reference's kernelK sweep
 // (src/simulator-mpi/kernels/nointrin/kernel5.hpp:1134-1193) and the diagonal
 // sweeps (kernels_diag.hpp:20-81). Two instances: complex128 states (below)
-// and complex64 states (three digits per real, levels 0-3, all exact; see
-// the complex64 section).
+// and complex64 states (three digits per state real, four per gate real,
+// levels 0-3, all exact; see the complex64 section).
 //
 // Tile: 4096 amplitudes = 128 index groups x 32 inputs (the five target bits).
 // Per tile the gate is the real GEMM Y[128 x 64] = X[128 x 64] B[64 x 64]
@@ -76,7 +76,7 @@ struct Lay<false> {  // complex128
 template <>
 struct Lay<true> {  // complex64
     static constexpr int kDigits = 3;
-    static constexpr uint32_t kGate = 0;         // 3 gate digit planes + a zero plane, 64 rows x 128 B each
+    static constexpr uint32_t kGate = 0;         // 4 gate digit planes, 64 rows x 128 B each
     static constexpr uint32_t kGateBytes = kUmmaGatePlaneBytes64;
     static constexpr uint32_t kPlanes = 0;       // (state planes all in tensor memory)
     static constexpr uint32_t kTile0 = 32768;    // tile buffers, 4096 x float2
@@ -321,15 +321,15 @@ __device__ __forceinline__ void run_apply(double2* buf, const float4* tab, const
 // digits relative to its group's largest float exponent Ef (X' = x 2^k,
 // k = min(134 - Ef, 126), |X'| < 2^8: d0 = X' rounded to an integer, then two
 // more rounded 9-bit digits, X' to 2^-19, 2^-27 of the group's scale), every
-// gate real as three digits relative to its column (|B'| < 2^7, top digit
-// <= 128). The products with i + j = 0..3 go to four FP32 accumulator
-// regions; every level sum stays below 2^24 (level 2, the largest:
-// 64 (256^2 + 256^2 + 256 * 128) < 2^23.4), so the accumulators hold exact
+// gate real as four digits relative to its column (|B'| < 2^7, top digit
+// <= 128; the gate to 2^-35 of its column's scale). The products with
+// i + j = 0..3 go to four FP32 accumulator regions; every level sum stays
+// below 2^24 (levels 2 and 3, the largest: 64 (256^2 + 256^2 + 256 * 128)
+// and 64 * 3 * 256^2, below 2^23.6), so the accumulators hold exact
 // integers and the tensor cores' rounding of their accumulation never
-// applies. The dropped level 4 (d2 e2) is below 2^-34 of the
-// row-times-column scale. The output is sum_L S_L 2^(-9 L) by an FMA chain
-// (error below 2^-23 of sum_k |x_k b_kn|), times the column's and the
-// group's scale.
+// applies. The dropped levels 4-5 are below 2^-34 of the row-times-column
+// scale. The output is sum_L S_L 2^(-9 L) by an FMA chain (error below
+// 2^-23 of sum_k |x_k b_kn|), times the column's and the group's scale.
 
 // X' = x 2^k; each digit rounds with the magic-number add folded into an FMA
 // (the product by 512 is exact, so the FMA rounds once, to an integer)
@@ -552,8 +552,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
                     auto td = [&](int lev) { return tmem + (uint32_t)lev * 64u; };
                     const uint32_t acc0 = ks > 0 ? 1u : 0u;
                     if constexpr (C64) {
-                        // gate plane 3 is zero: the first MMA also clears level 3
-                        mma_ts(td(0), ta(0), gdesc(0), idesc256, acc0);  // levels 0-3
+                        mma_ts(td(0), ta(0), gdesc(0), idesc256, acc0);  // levels 0-3 (gate digits 0-3)
                         mma_ts(td(1), ta(1), gdesc(0), idesc192, 1u);    // levels 1-3
                         mma_ts(td(2), ta(2), gdesc(0), idesc128, 1u);    // levels 2-3
                     } else {
@@ -772,7 +771,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             if (threadIdx.x == 0) mbar_arrive(&tdone[s]);
         }
     } else {
-        // ---- compute warps (complex64): three digits per real (exact
+        // ---- compute warps (complex64): three digits per state real (exact
         // levels 0-3), runs in FP32 complex, outputs rounded to float
         const int q4 = warp & 3, part = warp >> 2, g = q4 * 32 + lane;
         const OpDesc& tc = d.ops[u.tc_op];

@@ -505,8 +505,8 @@ static size_t ew_pool_bytes(const GateOp& op, int arith) { return op.m.size() * 
 // a = rint(|v| 2^(1074 - ebmax)) (to nearest, ties to even; a < 2^52) cut
 // into 9-bit fields, balanced into [-256, 255] with carries upward (the top
 // digit ends at most 128), then given v's sign.
-// With nd = 3 (complex64) the same column scale keeps the top three digits:
-// a = rint(|v| 2^(1047 - ebmax)) < 2^25.
+// With nd = 4 (complex64) the same column scale keeps the top four digits:
+// a = rint(|v| 2^(1056 - ebmax)) < 2^34.
 static void gate_digits9(double v, int ebmax, int nd, int (&d)[6]) {
     uint64_t u;
     std::memcpy(&u, &v, 8);
@@ -534,8 +534,8 @@ static void gate_digits9(double v, int ebmax, int nd, int (&d)[6]) {
 // that are not the gate's targets), in real form B[k][n] (k = 2c + part of
 // input c, n = 2r + part of output r), as six digit planes (plane j: rows
 // n = 0..63 of 64 fp16 over k, K-major with the 128-byte swizzle of the MMA
-// operand), then the 64 column exponents as int32. complex64: three digit
-// planes and a fourth of zeros.
+// operand), then the 64 column exponents as int32. complex64: four digit
+// planes.
 static void build_umma_gate(const GateOp& g, const int (&pos5)[5], bool c64, unsigned char* dst) {
     int realbit[5];
     for (int j = 0; j < 5; ++j) {
@@ -564,7 +564,7 @@ static void build_umma_gate(const GateOp& g, const int (&pos5)[5], bool c64, uns
         return pout == 0 ? -m.imag() : m.real();
     };
     const uint32_t plane_bytes = c64 ? kUmmaGatePlaneBytes64 : kUmmaGatePlaneBytes;
-    const int nd = c64 ? 3 : 6;
+    const int nd = c64 ? 4 : 6;
     uint16_t* planes = reinterpret_cast<uint16_t*>(dst);
     std::memset(planes, 0, plane_bytes);
     int32_t* ecol = reinterpret_cast<int32_t*>(dst + plane_bytes);

@@ -53,8 +53,8 @@ extern "C" {
                             products are summed apart and added with round-to-nearest, which
                             leaves a norm loss of about 7e-8 per dense 5-qubit gate (measured). */
 #define HQS_ARITH_TC64 6 /* complex64: dense 3-5 qubit gates as exact fp16 digit products on the
-                            tensor cores (three digits per real in the tensor-memory pass from
-                            12 qubits, exact levels: no norm drift; two digits below 12 qubits
+                            tensor cores (3 state x 4 gate digits in the tensor-memory pass from
+                            12 qubits, exact levels: no truncation bias; two digits below 12 qubits
                             and in serving batches), everything else FP32. hqs_sim / hqs_server
                             map HQS_ARITH_TC with HQS_C64 to this. */
 

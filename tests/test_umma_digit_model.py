@@ -297,17 +297,17 @@ def level_sum4_scaled(S, k, ebc):
     return F(F(float(v) * cs) * F(2.0 ** -k))
 
 
-def gate_digits3(v, ebmax):
-    """workspace.cpp gate_digits9 with nd = 3."""
+def gate_digits4(v, ebmax):
+    """workspace.cpp gate_digits9 with nd = 4 (complex64)."""
     u = _bits(v)
     eb = (u >> 52) & 0x7FF
     a = 0
-    sh = ebmax - eb + 1 + 27
+    sh = ebmax - eb + 1 + 18
     if eb and sh < 62:
         m = (u & ((1 << 52) - 1)) | (1 << 52)
         a = (m + (1 << (sh - 1)) - 1 + ((m >> sh) & 1)) >> sh
-    r = [a >> 18, (a >> 9) & 511, a & 511]
-    for i in (2, 1):
+    r = [a >> 27, (a >> 18) & 511, (a >> 9) & 511, a & 511]
+    for i in (3, 2, 1):
         c = (r[i] + 256) >> 9
         r[i] -= c << 9
         r[i - 1] += c
@@ -315,8 +315,8 @@ def gate_digits3(v, ebmax):
 
 
 def test_umma_complex64_digits_levels_and_outputs():
-    """complex64 tensor-memory pass: three state and three gate digits per
-    real, levels 0-3 exact (every level sum below 2^24, also for flat rows
+    """complex64 tensor-memory pass: three digits per state real and four
+    per gate real, levels 0-3 exact (every level sum below 2^24, also for flat rows
     against flat columns); the output (level sums by an FMA chain, times the
     column and group scales)'s error against the exact product of
     the same float inputs and double gate entries is below 2^-23 of
@@ -339,11 +339,11 @@ def test_umma_complex64_digits_levels_and_outputs():
         assert all(abs(d) <= 256 for dd in dx for d in dd)
         for n in range(0, 64, 5):
             ebc = max((_bits(b[k, n]) >> 52) & 0x7FF for k in range(64))
-            de = [gate_digits3(b[k, n], ebc) for k in range(64)]
-            assert all(abs(e[0]) <= 128 and abs(e[1]) <= 256 and abs(e[2]) <= 256 for e in de)
+            de = [gate_digits4(b[k, n], ebc) for k in range(64)]
+            assert all(abs(e[0]) <= 128 and max(abs(t) for t in e[1:]) <= 256 for e in de)
             S = [0] * 4
             for i in range(3):
-                for j in range(3):
+                for j in range(4):
                     if i + j <= 3:
                         S[i + j] += sum(dx[k][i] * de[k][j] for k in range(64))
             assert all(abs(v) < 1 << 24 for v in S), S
