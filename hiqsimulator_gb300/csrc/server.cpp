@@ -172,6 +172,46 @@ void Server::prepare(Prep& p) const {
     // gate's occupancy: their digit scratch grows with the tile, and a batched
     // launch runs at its largest item's (measured: 109 circuits/s against 104
     // at a floor of 2 CTAs per SM and 86 with no floor)
+    // complex128 states of kServeUmmaBits qubits or more: every dense
+    // 3-5-qubit gate as a tensor-memory launch of its own (with the diagonal
+    // runs around it), the other gates in batched tiled passes. complex64
+    // states stay batched: their two-digit tiled passes are cheap enough that
+    // one launch per state costs more (measured: 179 against 281 circuits/s)
+    if (arith_ == kArithTC && p.n >= kServeUmmaBits && umma_enabled()) {
+        std::vector<LaunchPlan> L = plan_launches(p.n, arith_, ops, kMaxTileBits, kMaxOpsPerPass, true);
+        size_t total = 0;
+        for (auto& l : L) {
+            total = (total + 1023) & ~(size_t)1023;
+            l.pool_off = total;
+            total += (l.pool_bytes + 255) & ~(size_t)255;
+        }
+        p.pool.assign(std::max<size_t>(total, 256), 0);
+        const size_t K = L.size();
+        p.plans.resize(K);
+        p.plan_tc.assign(K, 0);
+        p.plan_smem.assign(K, 0);
+        p.plan_umma.assign(K, 0);
+        p.plan_udesc.resize(K);
+        p.plan_pool.assign(K, 0);
+        for (size_t k = 0; k < K; ++k) {
+            p.plan_pool[k] = (uint32_t)L[k].pool_bytes;
+            if (L[k].umma) {
+                p.plan_umma[k] = 1;
+                p.plan_udesc[k] = L[k].udesc;
+                p.plans[k].pool_off = L[k].pool_off;
+                write_umma_pool(L[k].udesc, ops.data() + L[k].first, p.pool.data() + L[k].pool_off);
+                continue;
+            }
+            p.plans[k] = L[k].pass;
+            p.plans[k].pool_off = L[k].pool_off;
+            PassDesc& d = p.plans[k].desc;
+            d.prefetch = 0;  // the batched kernel loads its tiles directly
+            write_pass_pool(arith_, d, ops.data() + L[k].first, p.pool.data() + L[k].pool_off);
+            p.plan_tc[k] = pass_has_tc(d) ? 1 : 0;
+            p.plan_smem[k] = (uint32_t)pass_smem_bytes(arith_, d);
+        }
+        return;
+    }
     std::vector<size_t> first;
     p.plans = plan_passes(p.n, arith_, ops.data(), ops.size(), kMaxTileBits, kMaxOpsPerPass, &first, SIZE_MAX,
                           arith_ == kArithTC ? -1 : 0);
@@ -180,6 +220,7 @@ void Server::prepare(Prep& p) const {
     p.pool.assign(total, 0);
     p.plan_tc.resize(p.plans.size());
     p.plan_smem.resize(p.plans.size());
+    p.plan_umma.assign(p.plans.size(), 0);
     for (size_t k = 0; k < p.plans.size(); ++k) {
         PassDesc& d = p.plans[k].desc;
         d.prefetch = 0;  // the batched kernel loads its tiles directly
@@ -289,6 +330,9 @@ ServerResult Server::finish(Req& r) {
         }
         res.value_re = out;
     }
+    bool failed = false;  // a tensor-memory launch's bounded wait ran out
+    cuda_check(umma_check_error(&failed), "umma_check_error");
+    if (failed) throw CudaError("tensor-memory pass: a bounded device wait ran out (results of the pass are invalid)");
     cuda_check(cudaFreeAsync(r.state, s), "cudaFreeAsync");
     r.state = nullptr;
     bytes_in_use_ -= r.bytes;
@@ -314,10 +358,12 @@ std::vector<ServerResult> Server::step() {
         bool tc;
         size_t smem;
     };
-    std::vector<Planned> planned;
+    std::vector<Planned> planned, umma;
     for (auto& r : active_) {
         if (r.next >= r.prep->plans.size()) continue;
-        planned.push_back(Planned{&r, r.next, r.prep->plan_tc[r.next] != 0, r.prep->plan_smem[r.next]});
+        const Planned pl{&r, r.next, r.prep->plan_tc[r.next] != 0, r.prep->plan_smem[r.next]};
+        if (r.prep->plan_umma[r.next]) umma.push_back(pl);
+        else planned.push_back(pl);
         ++r.next;
         ++r.passes;
     }
@@ -328,13 +374,9 @@ std::vector<ServerResult> Server::step() {
         if (a.tc != b.tc) return a.tc > b.tc;
         return smem_class(a.smem) < smem_class(b.smem);
     });
-    auto launch = [&](size_t lo, size_t hi) {
-        const bool tc = planned[lo].tc;
-        const size_t nitems = hi - lo;
-        const size_t head = ((nitems * sizeof(BatchItem)) + 255) & ~(size_t)255;
-        size_t total = head;
-        for (size_t i = lo; i < hi; ++i)
-            total += pass_pool_bytes(arith_, planned[i].r->prep->plans[planned[i].k].desc);
+    // one of the two pinned staging buffers and its device copy, at least
+    // total bytes, once the copy that last used it has finished
+    auto staging = [&](size_t total, unsigned char*& host, unsigned char*& dev) {
         const int f = flip_;
         flip_ ^= 1;
         const double tw = now();
@@ -355,8 +397,41 @@ std::vector<ServerResult> Server::step() {
             cuda_check(cudaMalloc(&dev_[f], total * 2), "cudaMalloc(batch)");
             dev_bytes_[f] = total * 2;
         }
-        unsigned char* host = static_cast<unsigned char*>(staging_[f]);
-        unsigned char* dev = static_cast<unsigned char*>(dev_[f]);
+        host = static_cast<unsigned char*>(staging_[f]);
+        dev = static_cast<unsigned char*>(dev_[f]);
+        return f;
+    };
+    // tensor-memory launches: one per large state, pools staged together
+    if (!umma.empty()) {
+        size_t total = 0;
+        for (const auto& u : umma) total += (u.r->prep->plan_pool[u.k] + 1023) & ~(size_t)1023;
+        unsigned char *host = nullptr, *dev = nullptr;
+        const int f = staging(total, host, dev);
+        size_t off = 0;
+        const double tl = now();
+        for (const auto& u : umma) {
+            std::memcpy(host + off, u.r->prep->pool.data() + u.r->prep->plans[u.k].pool_off, u.r->prep->plan_pool[u.k]);
+            off += (u.r->prep->plan_pool[u.k] + 1023) & ~(size_t)1023;
+        }
+        cuda_check(cudaMemcpyAsync(dev, host, total, cudaMemcpyHostToDevice, s), "cudaMemcpyAsync(umma)");
+        cuda_check(cudaEventRecord(staging_done_[f], s), "cudaEventRecord");
+        off = 0;
+        for (const auto& u : umma) {
+            cuda_check(launch_umma_pass(u.r->state, dev + off, u.r->prep->plan_udesc[u.k], s), "launch_umma_pass");
+            off += (u.r->prep->plan_pool[u.k] + 1023) & ~(size_t)1023;
+            ++launches_;
+        }
+        t_phase_[2] += now() - tl;
+    }
+    auto launch = [&](size_t lo, size_t hi) {
+        const bool tc = planned[lo].tc;
+        const size_t nitems = hi - lo;
+        const size_t head = ((nitems * sizeof(BatchItem)) + 255) & ~(size_t)255;
+        size_t total = head;
+        for (size_t i = lo; i < hi; ++i)
+            total += pass_pool_bytes(arith_, planned[i].r->prep->plans[planned[i].k].desc);
+        unsigned char *host = nullptr, *dev = nullptr;
+        const int f = staging(total, host, dev);
         BatchItem* bi = reinterpret_cast<BatchItem*>(host);
         size_t off = head;
         uint64_t tiles = 0;

@@ -53,6 +53,11 @@ struct ServerResult {
     uint32_t passes;                // fused passes the circuit took
 };
 
+// Serving complex128 states of this many qubits or more run their dense
+// gates as tensor-memory launches (one per state per round; 64 or more tiles
+// of 4096 amplitudes); smaller states stay in the batched tiled launches.
+constexpr int kServeUmmaBits = 18;
+
 class Server {
 public:
     Server(int precision, int arith, uint64_t budget_bytes, int max_active, int cluster_size);
@@ -96,6 +101,12 @@ private:
         std::vector<PassPlan> plans;
         std::vector<uint8_t> plan_tc;      // pass runs tensor-core gates
         std::vector<uint32_t> plan_smem;   // shared-memory bytes of the pass
+        // tensor-memory launches (complex128 states of kServeUmmaBits qubits
+        // or more): the launch's descriptor and pool bytes (its pool at
+        // plans[k].pool_off)
+        std::vector<uint8_t> plan_umma;
+        std::vector<UmmaDesc> plan_udesc;
+        std::vector<uint32_t> plan_pool;
         std::vector<unsigned char> pool;
         std::exception_ptr error;
         std::atomic<bool> ready{false};

@@ -105,3 +105,51 @@ def test_poisson_serving_reports_latency(hqs, cuda):
     res1, st1 = serving.serve(circuits, arr, budget_bytes=1 << 30, max_active=1)
     for i in range(len(circuits)):
         assert (res[i]["value_re"], res[i]["sample"]) == (res1[i]["value_re"], res1[i]["sample"])
+
+
+@pytest.mark.parametrize("precision", ["c128", "c64"])
+def test_large_states_in_tensor_memory_launches(hqs, cuda, oracle_lib, precision):
+    """complex128 states of 18 qubits or more run their dense gates as
+    tensor-memory launches inside the rounds, next to the batched small
+    states (complex64 states stay batched): results are the same alone and
+    in the mix, and (complex128) match the oracle."""
+    from hiqsimulator_gb300 import serving
+    large = serving.serving_workload(21, 4, nmin=18, nmax=19, dmin=3, dmax=5)
+    circuits = large + _mix(22, 8)
+    alone = {}
+    for idx in (0, 1):
+        srv = serving.Server(precision, "auto", budget_bytes=1 << 32)
+        srv.submit(circuits[idx])
+        alone[idx] = srv.drain()[0]
+        srv.close()
+    srv = serving.Server(precision, "auto", budget_bytes=1 << 32)
+    ids = {srv.submit(c): i for i, c in enumerate(circuits)}
+    mixed = {ids[r["id"]]: r for r in srv.drain()}
+    assert srv.info()["launches"] > 0
+    for idx, r in alone.items():
+        m = mixed[idx]
+        assert (r["value_re"], r["value_im"], r["sample"]) == (m["value_re"], m["value_im"], m["sample"]), idx
+    if precision != "c128":
+        return
+    for i in range(2):
+        c = circuits[i]
+        sim = _oracle_result(c)
+        r = mixed[i]
+        if c.kind == serving.RESULT_AMPLITUDE0:
+            assert abs(complex(r["value_re"], r["value_im"]) - sim.vec[0]) < 1e-12
+        elif c.kind == serving.RESULT_SAMPLE:
+            assert r["sample"] == sim.sample_index(c.rnd)
+        else:
+            op = []
+            for x, y, z, coef in c.pauli:
+                term = []
+                for q in range(c.n):
+                    b = 1 << q
+                    if y & b:
+                        term.append((q, "Y"))
+                    elif x & b:
+                        term.append((q, "X"))
+                    elif z & b:
+                        term.append((q, "Z"))
+                op.append((term, coef))
+            assert abs(r["value_re"] - sim.get_expectation_value(op, list(range(c.n)))) < 1e-11
