@@ -246,12 +246,13 @@ __device__ __forceinline__ void level_sum_to_df(const float (&S)[6], float& h, f
 }
 
 // The double nearest (h + l) 2^off for a normalized double-float, assembled
-// with integer operations (0 below the double range).
+// with integer operations, without branches (0 for h = 0 and below the
+// double range).
 __device__ __forceinline__ double df_to_double_scaled(float h, float l, int off) {
     const uint32_t hb = __float_as_uint(h);
     const int eh = (int)((hb >> 23) & 0xFFu);
     const int be = eh + 896 + off;
-    if (eh == 0 || be <= 0) return 0.0;
+    const unsigned long long keep = (eh == 0 || be <= 0) ? 0ULL : ~0ULL;
     const uint32_t sg = hb & 0x80000000u;
     const uint32_t whi = ((uint32_t)be << 20) | ((hb & 0x7FFFFFu) >> 3) | sg;
     const uint32_t wlo = hb << 29;
@@ -266,7 +267,7 @@ __device__ __forceinline__ double df_to_double_scaled(float h, float l, int off)
     // magnitude bits plus the signed correction, sign bit kept
     w = (w & 0x7FFFFFFFFFFFFFFFULL) + (unsigned long long)(long long)delta;
     w |= (unsigned long long)sg << 32;
-    return __longlong_as_double((long long)w);
+    return __longlong_as_double((long long)(w & keep));
 }
 
 // ------------------------------------------------------------------ element-wise runs
@@ -755,10 +756,11 @@ __global__ void __launch_bounds__(kThreadsU, 1)
                             l[0] = v.z;
                             l[1] = v.w;
                         }
-                        const int c0 = a * 2;
-                        buf[L] = Eb == 0 ? make_double2(0.0, 0.0)
-                                         : make_double2(df_to_double_scaled(h[0], l[0], Eb + ecol[n0 + c0] - 2059),
-                                                        df_to_double_scaled(h[1], l[1], Eb + ecol[n0 + c0 + 1] - 2059));
+                        // a zero group (Eb = 0): the offset puts every output below
+                        // the double range, so it is 0 (no branch)
+                        const int c0 = a * 2, ez = Eb == 0 ? -4096 : 0;
+                        buf[L] = make_double2(df_to_double_scaled(h[0], l[0], Eb + ez + ecol[n0 + c0] - 2059),
+                                              df_to_double_scaled(h[1], l[1], Eb + ez + ecol[n0 + c0 + 1] - 2059));
                     }
                     if (ch < 3) tmem_ld_wait_regs(r[ch + 1]);
                 }
