@@ -24,7 +24,11 @@
 // swizzle); the gate's six digit planes are operand B (N = 64 outputs per
 // digit, shared memory). X_i times the gate planes j = 0..5-i, placed side by
 // side along N, accumulates each (i, j) product directly into the region of
-// level i + j: one MMA covers up to four levels (N = 256).
+// level i + j: one MMA covers up to four levels (N = 256). A pass that holds
+// only the dense gate does the outputs in two halves of 32 instead (level
+// regions of 32 columns, the gate's rows ordered by half, one MMA per X_i and
+// half), each half's MMAs committed to their own barrier: the compute warps
+// assemble the first half's outputs while the second half's MMAs run.
 //
 // Warps: 0-15 split digits and assemble outputs (CUDA cores; four per warp
 // scheduler), warp 16 moves tiles with TMA tensor copies (load into one of
@@ -70,7 +74,7 @@ struct Lay<false> {  // complex128
     static constexpr uint32_t kTile1 = 147456;
     static constexpr uint32_t kTileBytes = 4096 * 16;
     static constexpr uint32_t kEcol = 212992;
-    static constexpr uint32_t kTmPlanes = 384;   // tensor-memory columns: six level regions of 64, then planes 0-3
+    static constexpr uint32_t kTmPlanes = 384;   // tensor-memory columns: six level regions of 64 (or per output half six of 32), then planes 0-3
     static constexpr uint32_t kTabEntry = 16;    // factor-table entry: double-float complex
 };
 template <>
@@ -94,7 +98,7 @@ struct Sm : Lay<C64> {
     static constexpr uint32_t kMx = kErow + 512;    // uint32[512]: quarter-group maxima
     static constexpr uint32_t kGb = kMx + 2048;     // uint16[128]: tile index of each group's input 0
     static constexpr uint32_t kOff = kGb + 256;     // uint16[32]: tile offset of each input
-    static constexpr uint32_t kBar = kOff + 64;     // 6 mbarriers
+    static constexpr uint32_t kBar = kOff + 64;     // 7 mbarriers
     static constexpr uint32_t kMisc = kBar + 64;    // tensor-memory base, abort flag
     static constexpr uint32_t kLut = kMisc + 64;    // uint8[2][2][64]: factor-table index of tile slots 0-5 / 6-11
     static constexpr uint32_t kTab = kLut + 256;    // [2][256] factor tables of the current tile
@@ -397,6 +401,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
     uint64_t* tdone = bars + 2;   // [2] tile computed
     uint64_t* pbar = bars + 4;    // state digits written
     uint64_t* mbar = bars + 5;    // MMAs complete
+    uint64_t* mbar0 = bars + 6;   // output halves: MMAs of outputs 0-31 complete
     uint32_t* tmem_s = reinterpret_cast<uint32_t*>(sm + S::kMisc);
     volatile int* abort = reinterpret_cast<volatile int*>(sm + S::kMisc + 8);
     int* erow = reinterpret_cast<int*>(sm + S::kErow);
@@ -411,7 +416,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
 
     // ---- set-up
     if (threadIdx.x == 0) {
-        for (int i = 0; i < 6; ++i) mbar_init(&bars[i], 1);
+        for (int i = 0; i < 7; ++i) mbar_init(&bars[i], 1);
         *abort = 0;
         mbar_init_fence();
     }
@@ -534,9 +539,12 @@ __global__ void __launch_bounds__(kThreadsU, 1)
         __syncwarp();
     } else if (warp == kMmaWarp) {
         // ---- MMA issue
-        const uint32_t idesc256 = idesc_f16(128, 256), idesc192 = idesc_f16(128, 192),
-                       idesc128 = idesc_f16(128, 128), idesc64 = idesc_f16(128, 64);
+        const uint32_t idesc256 = idesc_f16(128, 256), idesc192 = idesc_f16(128, 192), idesc160 = idesc_f16(128, 160),
+                       idesc128 = idesc_f16(128, 128), idesc96 = idesc_f16(128, 96), idesc64 = idesc_f16(128, 64),
+                       idesc32 = idesc_f16(128, 32);
         const uint32_t gate = smem_u32(sm + S::kGate), planes = smem_u32(sm + S::kPlanes);
+        // complex128 passes that hold only the dense gate: outputs in two halves
+        const bool halves = !C64 && d.nops == 1;
         uint64_t committed = 0;
         for (uint64_t it = 0; it < my_n; ++it) {
             bool ok = true;
@@ -544,7 +552,27 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
             if (!ok) break;
             fence_after_sync();
-            if (lane == 0) {
+            if (lane == 0 && halves) {
+                // outputs 0-31, then 32-63: per half six level regions of 32
+                // columns and the gate rows of the half (six planes of 32
+                // rows), so that X_i times gate digits 0..5-i is one MMA
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+#pragma unroll
+                    for (int ks = 0; ks < 4; ++ks) {
+                        const uint64_t g0 = sdesc_sw128(gate + (uint32_t)h * 24576u + (uint32_t)ks * 32u);
+                        auto ta = [&](int i) { return tmem + S::kTmPlanes + (uint32_t)i * 32u + (uint32_t)ks * 8u; };
+                        auto td = [&](int lev) { return tmem + (uint32_t)h * 192u + (uint32_t)lev * 32u; };
+                        mma_ts(td(0), ta(0), g0, idesc192, ks > 0 ? 1u : 0u);  // levels 0-5
+                        mma_ts(td(1), ta(1), g0, idesc160, 1u);                // levels 1-5
+                        mma_ts(td(2), ta(2), g0, idesc128, 1u);                // levels 2-5
+                        mma_ts(td(3), ta(3), g0, idesc96, 1u);                 // levels 3-5
+                        mma_ss(td(4), sdesc_sw128(planes + (uint32_t)ks * 32u), g0, idesc64, 1u);           // levels 4-5
+                        mma_ss(td(5), sdesc_sw128(planes + 16384u + (uint32_t)ks * 32u), g0, idesc32, 1u);  // level 5
+                    }
+                    mma_commit(h == 0 ? mbar0 : mbar);
+                }
+            } else if (lane == 0) {
 #pragma unroll
                 for (int ks = 0; ks < 4; ++ks) {
                     // X_i times gate digits j0.. accumulates at level region i + j0
@@ -589,7 +617,7 @@ __global__ void __launch_bounds__(kThreadsU, 1)
         const int q4 = warp & 3, part = warp >> 2, g = q4 * 32 + lane;
         const OpDesc& tc = d.ops[u.tc_op];
         const uint32_t lane_base = (uint32_t)(q4 * 32) << 16;
-        const bool pre = u.tc_op > 0, post = u.tc_op + 1 < d.nops;
+        const bool pre = u.tc_op > 0, post = u.tc_op + 1 < d.nops, halves = d.nops == 1;
         const int npre = pre ? 1 << __popc(u.run_mask[0]) : 0, npost = post ? 1 << __popc(u.run_mask[1]) : 0;
         float4* tab_pre = reinterpret_cast<float4*>(sm + S::kTab);
         float4* tab_post = tab_pre + (1 << kUmmaRunBits);
@@ -708,64 +736,139 @@ __global__ void __launch_bounds__(kThreadsU, 1)
             // while the MMAs run: this tile's post-run table, the next tile's pre-run table
             if (post) build_post(base);
             if (pre && it + 1 < my_n) build_pre(walk.after(base));
-            mbar_wait(mbar, (uint32_t)(it & 1), abort);
-            bar_sync(1, kCompute);
-            if (*abort) break;
-            fence_after_sync();
-            if (act) {
-                // outputs: group g, output reals 16 part .. 16 part + 15. The
-                // tensor-memory loads are warp-collective: every thread takes
-                // part, also for a group that keeps its inputs.
-                const int Eb = erow[g];
-                // four chunks of four output reals; the next chunk's loads are
-                // in flight while the current one is assembled
-                uint32_t r[4][6][4];
-#pragma unroll
-                for (int lev = 0; lev < 6; ++lev) tmem_ld4(tmem + lane_base + (uint32_t)lev * 64u + (uint32_t)(part * 16), r[0][lev]);
-                tmem_ld_wait_regs(r[0]);
-#pragma unroll
-                for (int ch = 0; ch < 4; ++ch) {
-                    const uint32_t n0 = (uint32_t)(part * 16 + ch * 4);
-                    if (ch < 3) {
-#pragma unroll
-                        for (int lev = 0; lev < 6; ++lev)
-                            tmem_ld4(tmem + lane_base + (uint32_t)lev * 64u + n0 + 4u, r[ch + 1][lev]);
+            if (halves) {
+                // output halves (a pass without runs): outputs 0-31 as soon as
+                // their MMAs are complete, while the MMAs of outputs 32-63 run,
+                // then outputs 32-63
+                bool stop = false;
+    #pragma unroll 1
+                for (int h = 0; h < 2; ++h) {
+                    {
+                        mbar_wait(h == 0 ? mbar0 : mbar, (uint32_t)(it & 1), abort);
+                        bar_sync(1, kCompute);
+                        if (*abort) {
+                            stop = true;
+                            break;
+                        }
+                        fence_after_sync();
                     }
-#pragma unroll
-                    for (int a = 0; a < 2; ++a) {
-                        const uint32_t L = gbase | offt[(n0 >> 1) + a];
-                        if (!write) {  // the pre-run was stored with the digits
-                            if (post)
-                                buf[L] = ArithDFRaw::elem_store(
-                                    ArithDF::mul(tab_post[run_index(lut_post, L)], ArithDFRaw::elem_load(buf[L])));
-                            continue;
+                    if (!act) continue;
+                    // group g, output reals nb = 32 h + 8 part .. nb + 7 in two chunks
+                    // of four: the second chunk's loads are in flight while the
+                    // first is assembled. Level L of output n lies at column
+                    // 192 h + 32 L + n mod 32. The tensor-memory loads are
+                    // warp-collective: every thread takes part, also for a group
+                    // that keeps its inputs.
+                    const int Eb = erow[g];
+                    const uint32_t nb = (uint32_t)(h * 32 + part * 8);
+                    const uint32_t cb = lane_base + (uint32_t)(h * 192 + part * 8);
+                    constexpr uint32_t ls = 32u;
+                    uint32_t r[2][6][4];
+    #pragma unroll
+                    for (int lev = 0; lev < 6; ++lev) tmem_ld4(tmem + cb + (uint32_t)lev * ls, r[0][lev]);
+                    tmem_ld_wait_regs(r[0]);
+    #pragma unroll
+                    for (int ch = 0; ch < 2; ++ch) {
+                        const uint32_t n0 = nb + (uint32_t)(ch * 4);
+                        if (ch == 0) {
+    #pragma unroll
+                            for (int lev = 0; lev < 6; ++lev) tmem_ld4(tmem + cb + (uint32_t)lev * ls + 4u, r[1][lev]);
                         }
-                        float h[2], l[2];
-#pragma unroll
-                        for (int p = 0; p < 2; ++p) {
-                            const int c = a * 2 + p;
-                            const float S[6] = {__uint_as_float(r[ch][0][c]), __uint_as_float(r[ch][1][c]),
-                                                __uint_as_float(r[ch][2][c]), __uint_as_float(r[ch][3][c]),
-                                                __uint_as_float(r[ch][4][c]), __uint_as_float(r[ch][5][c])};
-                            level_sum_to_df(S, h[p], l[p]);
+    #pragma unroll
+                        for (int a = 0; a < 2; ++a) {
+                            const uint32_t L = gbase | offt[(n0 >> 1) + a];
+                            if (!write) {  // the pre-run was stored with the digits
+                                if (post)
+                                    buf[L] = ArithDFRaw::elem_store(
+                                        ArithDF::mul(tab_post[run_index(lut_post, L)], ArithDFRaw::elem_load(buf[L])));
+                                continue;
+                            }
+                            float hh[2], l[2];
+    #pragma unroll
+                            for (int p = 0; p < 2; ++p) {
+                                const int c = a * 2 + p;
+                                const float S[6] = {__uint_as_float(r[ch][0][c]), __uint_as_float(r[ch][1][c]),
+                                                    __uint_as_float(r[ch][2][c]), __uint_as_float(r[ch][3][c]),
+                                                    __uint_as_float(r[ch][4][c]), __uint_as_float(r[ch][5][c])};
+                                level_sum_to_df(S, hh[p], l[p]);
+                            }
+                            if (post) {
+                                const float4 v = ArithDF::mul(tab_post[run_index(lut_post, L)], make_float4(hh[0], hh[1], l[0], l[1]));
+                                hh[0] = v.x;
+                                hh[1] = v.y;
+                                l[0] = v.z;
+                                l[1] = v.w;
+                            }
+                            // a zero group (Eb = 0): the offset puts every output below
+                            // the double range, so it is 0 (no branch)
+                            const int c0 = a * 2, ez = Eb == 0 ? -4096 : 0;
+                            buf[L] = make_double2(df_to_double_scaled(hh[0], l[0], Eb + ez + ecol[n0 + c0] - 2059),
+                                                  df_to_double_scaled(hh[1], l[1], Eb + ez + ecol[n0 + c0 + 1] - 2059));
                         }
-                        if (post) {
-                            const float4 v = ArithDF::mul(tab_post[run_index(lut_post, L)], make_float4(h[0], h[1], l[0], l[1]));
-                            h[0] = v.x;
-                            h[1] = v.y;
-                            l[0] = v.z;
-                            l[1] = v.w;
-                        }
-                        // a zero group (Eb = 0): the offset puts every output below
-                        // the double range, so it is 0 (no branch)
-                        const int c0 = a * 2, ez = Eb == 0 ? -4096 : 0;
-                        buf[L] = make_double2(df_to_double_scaled(h[0], l[0], Eb + ez + ecol[n0 + c0] - 2059),
-                                              df_to_double_scaled(h[1], l[1], Eb + ez + ecol[n0 + c0 + 1] - 2059));
+                        if (ch == 0) tmem_ld_wait_regs(r[1]);
                     }
-                    if (ch < 3) tmem_ld_wait_regs(r[ch + 1]);
                 }
-            } else if (post) {
-                run_apply(buf, tab_post, lut_post);
+                if (stop) break;
+            } else {
+                mbar_wait(mbar, (uint32_t)(it & 1), abort);
+                bar_sync(1, kCompute);
+                if (*abort) break;
+                fence_after_sync();
+                if (act) {
+                    // outputs: group g, output reals 16 part .. 16 part + 15. The
+                    // tensor-memory loads are warp-collective: every thread takes
+                    // part, also for a group that keeps its inputs.
+                    const int Eb = erow[g];
+                    // four chunks of four output reals; the next chunk's loads are
+                    // in flight while the current one is assembled
+                    uint32_t r[4][6][4];
+    #pragma unroll
+                    for (int lev = 0; lev < 6; ++lev) tmem_ld4(tmem + lane_base + (uint32_t)lev * 64u + (uint32_t)(part * 16), r[0][lev]);
+                    tmem_ld_wait_regs(r[0]);
+    #pragma unroll
+                    for (int ch = 0; ch < 4; ++ch) {
+                        const uint32_t n0 = (uint32_t)(part * 16 + ch * 4);
+                        if (ch < 3) {
+    #pragma unroll
+                            for (int lev = 0; lev < 6; ++lev)
+                                tmem_ld4(tmem + lane_base + (uint32_t)lev * 64u + n0 + 4u, r[ch + 1][lev]);
+                        }
+    #pragma unroll
+                        for (int a = 0; a < 2; ++a) {
+                            const uint32_t L = gbase | offt[(n0 >> 1) + a];
+                            if (!write) {  // the pre-run was stored with the digits
+                                if (post)
+                                    buf[L] = ArithDFRaw::elem_store(
+                                        ArithDF::mul(tab_post[run_index(lut_post, L)], ArithDFRaw::elem_load(buf[L])));
+                                continue;
+                            }
+                            float h[2], l[2];
+    #pragma unroll
+                            for (int p = 0; p < 2; ++p) {
+                                const int c = a * 2 + p;
+                                const float S[6] = {__uint_as_float(r[ch][0][c]), __uint_as_float(r[ch][1][c]),
+                                                    __uint_as_float(r[ch][2][c]), __uint_as_float(r[ch][3][c]),
+                                                    __uint_as_float(r[ch][4][c]), __uint_as_float(r[ch][5][c])};
+                                level_sum_to_df(S, h[p], l[p]);
+                            }
+                            if (post) {
+                                const float4 v = ArithDF::mul(tab_post[run_index(lut_post, L)], make_float4(h[0], h[1], l[0], l[1]));
+                                h[0] = v.x;
+                                h[1] = v.y;
+                                l[0] = v.z;
+                                l[1] = v.w;
+                            }
+                            // a zero group (Eb = 0): the offset puts every output below
+                            // the double range, so it is 0 (no branch)
+                            const int c0 = a * 2, ez = Eb == 0 ? -4096 : 0;
+                            buf[L] = make_double2(df_to_double_scaled(h[0], l[0], Eb + ez + ecol[n0 + c0] - 2059),
+                                                  df_to_double_scaled(h[1], l[1], Eb + ez + ecol[n0 + c0 + 1] - 2059));
+                        }
+                        if (ch < 3) tmem_ld_wait_regs(r[ch + 1]);
+                    }
+                } else if (post) {
+                    run_apply(buf, tab_post, lut_post);
+                }
             }
             fence_proxy_async();
             fence_before_sync();

@@ -535,8 +535,10 @@ static void gate_digits9(double v, int ebmax, int nd, int (&d)[6]) {
 // input c, n = 2r + part of output r), as six digit planes (plane j: rows
 // n = 0..63 of 64 fp16 over k, K-major with the 128-byte swizzle of the MMA
 // operand), then the 64 column exponents as int32. complex64: four digit
-// planes.
-static void build_umma_gate(const GateOp& g, const int (&pos5)[5], bool c64, unsigned char* dst) {
+// planes. halves (complex128 passes that hold only the dense gate): the rows
+// ordered by output half, then plane (row 192 h + 32 j + n mod 32 for n in
+// half h = n / 32), so that one MMA covers all digit planes of a half.
+static void build_umma_gate(const GateOp& g, const int (&pos5)[5], bool c64, bool halves, unsigned char* dst) {
     int realbit[5];
     for (int j = 0; j < 5; ++j) {
         realbit[j] = -1;
@@ -576,7 +578,7 @@ static void build_umma_gate(const GateOp& g, const int (&pos5)[5], bool c64, uns
             int dg[6];
             gate_digits9(bval(kk, nn), ebmax, nd, dg);
             for (int j = 0; j < nd; ++j) {
-                const int row = 64 * j + nn;
+                const int row = halves ? 192 * (nn >> 5) + 32 * j + (nn & 31) : 64 * j + nn;
                 const size_t byte = (size_t)row * 128 + ((size_t)(((2 * kk) >> 4) ^ (row & 7)) << 4) + ((2 * kk) & 15);
                 planes[byte / 2] = half_of_int(dg[j]);
             }
@@ -747,7 +749,7 @@ void write_umma_pool(const UmmaDesc& u, const GateOp* ops, unsigned char* dst) {
     }
     int pos5[5];
     for (int j = 0; j < 5; ++j) pos5[j] = d.tile_pos[u.tslot[j]];
-    build_umma_gate(ops[u.tc_op], pos5, u.c64 != 0, dst + u.gate_off);
+    build_umma_gate(ops[u.tc_op], pos5, u.c64 != 0, !u.c64 && d.nops == 1, dst + u.gate_off);
 }
 
 std::vector<LaunchPlan> plan_launches(int n, int arith, const std::vector<GateOp>& ops, int max_tile_bits, int max_ops,
